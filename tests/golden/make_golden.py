@@ -1,0 +1,292 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference's own,
+unmodified RoadRunner Python code (hpparvi/PyTransit 2.8.1).
+
+Run in a container where the reference is checked out (default
+/root/reference, or pass its path as the first argument):
+
+    python tests/golden/make_golden.py [/path/to/PyTransit]
+
+numba and meepmeep are not installed, so the script puts two stand-ins from
+tests/golden/shim/ on sys.path: a pass-through ``numba`` (njit returns the
+function, prange is range) and a restated ``meepmeep.backends.numba.point2d``.
+It registers bare ``pytransit`` / ``pytransit.models`` package objects so that
+``pytransit/__init__.py`` (astropy, pandas, emcee ...) is not executed, and
+keeps Python's bytecode caches out of the reference tree.
+
+Everything except the orbit layer is therefore the reference's own code:
+RoadRunnerModel.__init__/set_data/evaluate (rrmodel.py), rr_full and rr_simple
+(model_full.py, model_simple.py), the weight tables, area and interpolation
+(common.py), the LD laws (numba/ldmodels.py), LDModel (ldmodel.py),
+TransitModel.set_data (transitmodel.py) and TransmissionSpectroscopyModel /
+tsmodel_serial (tsmodel.py, model_trspec.py).
+"""
+import os
+import sys
+import tempfile
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.path.abspath(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+
+
+def _setup_reference():
+    sys.pycache_prefix = tempfile.mkdtemp(prefix="golden_pycache_")
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, os.path.join(HERE, "shim"))
+    pkg = types.ModuleType("pytransit")
+    pkg.__path__ = [os.path.join(REF, "pytransit")]
+    sys.modules["pytransit"] = pkg
+    models = types.ModuleType("pytransit.models")
+    models.__path__ = [os.path.join(REF, "pytransit", "models")]
+    sys.modules["pytransit.models"] = models
+    pkg.models = models
+
+
+_setup_reference()
+
+from pytransit.models.roadrunner.rrmodel import RoadRunnerModel  # noqa: E402
+from pytransit.models.roadrunner.tsmodel import TransmissionSpectroscopyModel  # noqa: E402
+from pytransit.models.roadrunner import common as rrc  # noqa: E402
+from pytransit.models.ldmodel import LDModel  # noqa: E402
+from pytransit.models.numba import ldmodels as ldm  # noqa: E402
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **arrays)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.1f} KiB)")
+
+
+def draw_pv(rng, npv, p_range=(1.0, 10.0), ecc=False, t0c=0.0):
+    """Parameter vectors with the distributions of the small (64 x 1000) workload."""
+    k = rng.uniform(0.05, 0.15, npv)
+    u1 = rng.uniform(0.0, 0.6, npv)
+    u2 = rng.uniform(0.0, 0.3, npv)
+    t0 = t0c + rng.normal(0.0, 1e-3, npv)
+    p = rng.uniform(*p_range, npv)
+    a = rng.uniform(3.0, 20.0, npv)
+    b = rng.uniform(0.0, 0.9, npv)
+    inc = np.arccos(b / a)
+    if ecc:
+        e = rng.uniform(0.0, 0.3, npv)
+        w = rng.uniform(0.0, 2 * np.pi, npv)
+    else:
+        e = np.zeros(npv)
+        w = np.zeros(npv)
+    return k, u1, u2, t0, p, a, inc, e, w
+
+
+def case_c0():
+    """64 parameter vectors x 1000 times over t0 +- 0.15 d, quadratic LD, one LC."""
+    rng = np.random.default_rng(20240601)
+    npv = 64
+    time = np.linspace(-0.15, 0.15, 1000)
+    k, u1, u2, t0, p, a, inc, e, w = draw_pv(rng, npv)
+    ldc = np.stack([u1, u2], -1).reshape(npv, 1, 2)
+    tm = RoadRunnerModel('quadratic')
+    tm.set_data(time)
+    flux = tm.evaluate(k.reshape(npv, 1), ldc, t0.reshape(npv, 1), p, a, inc, e, w)
+    save("c0_quadratic", time=time, k=k.reshape(npv, 1), ldc=ldc, t0=t0.reshape(npv, 1), p=p, a=a,
+         inc=inc, e=e, w=w, flux=flux)
+
+
+def case_multi():
+    """Three light curves at BJD scale: two passbands, two epochs (TTV), mixed
+    supersampling, eccentric orbits, per-passband radius ratios, invalid rows."""
+    rng = np.random.default_rng(7)
+    T = 2459000.0
+    t_a = T + np.linspace(0.0, 10.0, 800)
+    t_b = T + np.linspace(0.003, 10.003, 700)
+    t_c = T + 20.0 + np.linspace(0.0, 6.0, 500)
+    time = np.concatenate([t_a, t_b, t_c])
+    lcids = np.concatenate([np.zeros(t_a.size, int), np.ones(t_b.size, int), np.full(t_c.size, 2)])
+    pbids = np.array([0, 1, 1])
+    epids = np.array([0, 0, 1])
+    nsamples = np.array([1, 5, 3])
+    exptimes = np.array([0.0, 0.02, 0.0104])
+    npv = 8
+    k = rng.uniform(0.07, 0.13, (npv, 2))
+    ldc = np.stack([rng.uniform(0, 0.6, (npv, 2)), rng.uniform(0, 0.3, (npv, 2))], -1)
+    t0 = T + 0.3 + rng.normal(0.0, 1e-3, npv)
+    t0 = np.stack([t0, t0 + rng.normal(0.0, 0.01, npv)], -1)
+    p = rng.uniform(1.0, 3.0, npv)
+    a = rng.uniform(4.0, 10.0, npv)
+    inc = np.arccos(rng.uniform(0.0, 0.95, npv) / a)
+    e = rng.uniform(0.0, 0.3, npv)
+    w = rng.uniform(0.0, 2 * np.pi, npv)
+    a[6] = 0.9      # a <= 1 -> NaN row
+    e[7] = -0.1     # e < 0 -> NaN row
+    tm = RoadRunnerModel('quadratic')
+    tm.set_data(time, lcids=lcids, pbids=pbids, nsamples=nsamples, exptimes=exptimes, epids=epids)
+    flux = tm.evaluate(k, ldc, t0, p, a, inc, e, w)
+    save("multi_lc_bjd", time=time, lcids=lcids, pbids=pbids, epids=epids, nsamples=nsamples,
+         exptimes=exptimes, k=k, ldc=ldc, t0=t0, p=p, a=a, inc=inc, e=e, w=w, flux=flux)
+
+
+def case_power2():
+    """Four BJD-scale light curves at 30-min cadence, nsamples = 10, power-2 LD,
+    eccentric orbits: a small instance of the precision workload."""
+    rng = np.random.default_rng(11)
+    T = 2459000.0
+    npts = np.exp(rng.uniform(np.log(150), np.log(500), 4)).astype(int)
+    time = np.concatenate([T + np.arange(n) / 48.0 for n in npts])
+    lcids = np.concatenate([np.full(n, j) for j, n in enumerate(npts)])
+    pbids = np.arange(4)
+    nsamples = np.full(4, 10)
+    exptimes = np.full(4, 1 / 48)
+    npv = 6
+    k, _, _, t0, p, a, inc, e, w = draw_pv(rng, npv, p_range=(0.5, 5.0), ecc=True, t0c=T)
+    c = rng.uniform(0.3, 0.9, (npv, 4))
+    al = rng.uniform(0.3, 0.8, (npv, 4))
+    ldc = np.stack([c, al], -1)
+    tm = RoadRunnerModel('power-2')
+    tm.set_data(time, lcids=lcids, pbids=pbids, nsamples=nsamples, exptimes=exptimes)
+    flux = tm.evaluate(k.reshape(npv, 1), ldc, t0.reshape(npv, 1), p, a, inc, e, w)
+    save("power2_ss10", time=time, lcids=lcids, pbids=pbids, nsamples=nsamples, exptimes=exptimes,
+         k=k.reshape(npv, 1), ldc=ldc, t0=t0.reshape(npv, 1), p=p, a=a, inc=inc, e=e, w=w, flux=flux)
+
+
+def case_laws():
+    """Every named LD law of the RoadRunner table on one small light curve,
+    including the ones without an analytic integral (200-point trapezoid)."""
+    rng = np.random.default_rng(3)
+    time = np.linspace(-0.2, 0.2, 300)
+    npv = 3
+    k, _, _, t0, p, a, inc, e, w = draw_pv(rng, npv, p_range=(1.0, 4.0), ecc=True)
+    coefs = {
+        'uniform': np.zeros((npv, 1, 1)),
+        'linear': rng.uniform(0.1, 0.6, (npv, 1, 1)),
+        'quadratic': np.stack([rng.uniform(0, .6, npv), rng.uniform(0, .3, npv)], -1).reshape(npv, 1, 2),
+        'quadratic-tri': rng.uniform(0.1, 0.9, (npv, 1, 2)),
+        'nonlinear': np.tile([0.5, -0.2, 0.6, -0.25], (npv, 1)).reshape(npv, 1, 4) * rng.uniform(0.8, 1.2, (npv, 1, 1)),
+        'general': rng.uniform(0.05, 0.2, (npv, 1, 3)),
+        'square_root': rng.uniform(0.1, 0.4, (npv, 1, 2)),
+        'logarithmic': rng.uniform(0.1, 0.4, (npv, 1, 2)),
+        'exponential': rng.uniform(0.05, 0.2, (npv, 1, 2)),
+        'power-2': np.stack([rng.uniform(.3, .9, npv), rng.uniform(.3, .8, npv)], -1).reshape(npv, 1, 2),
+        'power-2-pm': np.stack([rng.uniform(.5, .7, npv), rng.uniform(.2, .4, npv)], -1).reshape(npv, 1, 2),
+    }
+    out = dict(time=time, k=k.reshape(npv, 1), t0=t0.reshape(npv, 1), p=p, a=a, inc=inc, e=e, w=w)
+    for law, ldc in coefs.items():
+        tm = RoadRunnerModel(law)
+        tm.set_data(time)
+        out[f"ldc__{law}"] = ldc
+        out[f"flux__{law}"] = tm.evaluate(k.reshape(npv, 1), ldc, t0.reshape(npv, 1), p, a, inc, e, w)
+        out[f"mu__{law}"] = tm.mu
+        out[f"ldp__{law}"] = ldm.evaluate_ld(tm.ldmodel, tm.mu, ldc)
+    save("ld_laws", **out)
+
+
+class QuadLDModel(LDModel):
+    """A user LD model through the reference's LDModel protocol (ldmodel.py:21-38)."""
+
+    def _evaluate(self, mu, x):
+        x = np.asarray(x)
+        u1, u2 = x[..., 0:1], x[..., 1:2]
+        return 1.0 - u1 * (1.0 - mu) - u2 * (1.0 - mu) ** 2
+
+    def _integrate(self, x):
+        x = np.asarray(x)
+        return 2 * np.pi / 12 * (-2 * x[..., 0] - x[..., 1] + 6)
+
+
+def user_law(mu, pv):
+    return 1.0 - pv[0] * (1.0 - mu) - pv[1] * (1.0 - np.sqrt(mu))
+
+
+def case_user_ld():
+    """User-supplied LD: an LDModel instance, a bare callable (numerical disk
+    integral) and an (ld, ldi) tuple."""
+    rng = np.random.default_rng(5)
+    time = np.linspace(-0.2, 0.2, 300)
+    npv = 4
+    k, u1, u2, t0, p, a, inc, e, w = draw_pv(rng, npv, p_range=(1.0, 4.0))
+    ldc = np.stack([u1, u2], -1).reshape(npv, 1, 2)
+    out = dict(time=time, k=k.reshape(npv, 1), t0=t0.reshape(npv, 1), p=p, a=a, inc=inc, e=e, w=w, ldc=ldc)
+    for name, model in [("ldmodel", QuadLDModel()), ("callable", user_law),
+                        ("tuple", (ldm.ld_quadratic, ldm.ldi_quadratic))]:
+        tm = RoadRunnerModel(model)
+        tm.set_data(time)
+        out[f"flux__{name}"] = tm.evaluate(k.reshape(npv, 1), ldc, t0.reshape(npv, 1), p, a, inc, e, w)
+    save("user_ld", **out)
+
+
+def case_klims():
+    """Radius ratios outside the precomputed table (2D weight path)."""
+    time = np.linspace(-0.12, 0.12, 400)
+    k = np.array([[0.003], [0.6], [0.25], [0.005], [0.49]])
+    npv = k.shape[0]
+    ldc = np.tile([0.4, 0.2], (npv, 1)).reshape(npv, 1, 2)
+    t0 = np.zeros((npv, 1))
+    p = np.full(npv, 3.0)
+    a = np.full(npv, 8.0)
+    inc = np.arccos(np.array([0.1, 0.3, 0.5, 0.0, 0.2]) / a)
+    e = np.zeros(npv)
+    w = np.zeros(npv)
+    tm = RoadRunnerModel('quadratic')
+    tm.set_data(time)
+    flux = tm.evaluate(k, ldc, t0, p, a, inc, e, w)
+    save("klims", time=time, k=k, ldc=ldc, t0=t0, p=p, a=a, inc=inc, e=e, w=w, flux=flux)
+
+
+def case_simple():
+    """One parameter vector and one light curve: the rr_simple branch
+    (rrmodel.py:236-238), with supersampling."""
+    time = 2459000.0 + np.linspace(1.9, 2.1, 500)
+    tm = RoadRunnerModel('quadratic')
+    tm.set_data(time, nsamples=[4], exptimes=[0.01])
+    args = dict(k=0.11, ldc=np.array([0.35, 0.22]), t0=2459000.0 + 0.0004, p=2.0, a=6.5,
+                inc=np.arccos(0.4 / 6.5), e=0.12, w=1.3)
+    flux = tm.evaluate(args['k'], args['ldc'], args['t0'], args['p'], args['a'], args['inc'],
+                       args['e'], args['w'])
+    save("simple", time=time, flux=flux, **{k: np.asarray(v) for k, v in args.items()})
+
+
+def case_ts():
+    """TransmissionSpectroscopyModel: five channels sharing one orbit, with the
+    per-pv 2D table (default) and with the precomputed 3D table."""
+    rng = np.random.default_rng(13)
+    time = np.linspace(-0.2, 0.2, 500)
+    npv, npb = 3, 5
+    k = rng.uniform(0.09, 0.11, (npv, npb))
+    ldc = np.stack([rng.uniform(0.2, 0.5, (npv, npb)), rng.uniform(0.1, 0.3, (npv, npb))], -1)
+    t0 = rng.normal(0.0, 1e-3, npv)
+    p = rng.uniform(1.0, 4.0, npv)
+    a = rng.uniform(4.0, 12.0, npv)
+    inc = np.arccos(rng.uniform(0.0, 0.8, npv) / a)
+    e = rng.uniform(0.0, 0.2, npv)
+    w = rng.uniform(0.0, 2 * np.pi, npv)
+    out = dict(time=time, k=k, ldc=ldc, t0=t0, p=p, a=a, inc=inc, e=e, w=w)
+    for name, interp in [("2d", False), ("3d", True)]:
+        tm = TransmissionSpectroscopyModel('quadratic', precompute_weights=interp)
+        tm.set_data(time, nsamples=[3], exptimes=[0.01])
+        out[f"flux__{name}"] = tm.evaluate(k, ldc, t0, p, a, inc, e, w)
+    save("ts", **out)
+
+
+def case_tables():
+    """Integration grid, weight-table samples and the area/interpolation helpers."""
+    tm = RoadRunnerModel('quadratic')
+    W = tm.weights
+    rng = np.random.default_rng(17)
+    ks = rng.uniform(0.01, 0.6, 200)
+    zs = rng.uniform(0.0, 1.7, 200)
+    zs[:8] = [0.0, 0.1, 0.9, 1.0, 1.05, 1.1, 1.2, 0.5]
+    ks[:8] = [0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.6]
+    areas = np.array([rrc.circle_circle_intersection_area_kite(1.0, k, z) for k, z in zip(ks, zs)])
+    _, dg2, W2 = rrc.calculate_weights_2d(0.6, tm.ze, tm.ng)
+    lda = np.cos(np.linspace(0, 2, 100))
+    gs = np.concatenate([rng.uniform(0, 1.0 - 1e-6, 100), [0.0, 0.5, 1.0 + 1e-9, 1.2]])
+    interp = np.array([rrc.interpolate_mean_limb_darkening_s(g, tm.dg, lda) for g in gs])
+    save("tables", ze=tm.ze, zm=tm.zm, mu=tm.mu, dk=tm.dk, dg=tm.dg, w_sub=W[::37, ::9, :],
+         w_sum=W.sum(), w_sumsq=(W ** 2).sum(), w_rowsum=W.sum(-1), ks=ks, zs=zs, areas=areas,
+         dg2=dg2, w2=W2, lda=lda, gs=gs, interp=interp)
+
+
+if __name__ == "__main__":
+    for f in (case_tables, case_c0, case_multi, case_power2, case_laws, case_user_ld, case_klims,
+              case_simple, case_ts):
+        print(f.__name__)
+        f()
