@@ -1,0 +1,121 @@
+/*
+ * pytransit_gb300 — C ABI of the GB300-native RoadRunner transit-model path.
+ *
+ * Every entry point takes device pointers (allocated by the caller), plain
+ * sizes and a CUDA stream (as void*; NULL = legacy default stream), launches
+ * asynchronously on that stream and returns an int status (RR_OK = 0).  The
+ * library never allocates device memory: per-call scratch is a caller-owned
+ * workspace sized by the matching *_workspace_bytes() function.
+ *
+ * Array layouts are row-major, as the reference's numpy arrays:
+ *   times[npt] f64, k[npv, nkc] (nkc = 1 or npb), t0[npv, ldt0] (column =
+ *   epoch id), p/a/inc/e/w[npv] f64, lcids[npt] int32, pbids/epids/nsamples
+ *   [nlc] int32, exptimes[nlc] f64, ldp[npv, npb, nz], istar[npv, npb],
+ *   weights[nk, ng, nz], flux[npv, ldflux] (ldflux >= npt).
+ *
+ * Reference: hpparvi/PyTransit 2.8.1 (paths below are inside that project).
+ */
+#ifndef PYTRANSIT_GB300_H
+#define PYTRANSIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define RR_OK 0
+#define RR_ERR_SHAPE 1     /* k is neither [npv,1] nor [npv,npb] (model_full.py:18-19) */
+#define RR_ERR_ARG 2       /* a size or pointer argument is invalid */
+#define RR_ERR_WORKSPACE 3 /* workspace smaller than *_workspace_bytes() */
+#define RR_ERR_CUDA 4      /* a CUDA launch failed; see rr_last_cuda_error() */
+#define RR_ERR_LAW 5       /* unknown limb-darkening law id */
+#define RR_ERR_TIMEOUT 6   /* a bounded device wait ran out */
+
+/* Limb-darkening law ids: the named laws of RoadRunnerModel.ldmodels
+ * (pytransit/models/roadrunner/rrmodel.py:48-58). */
+#define RR_LD_UNIFORM 0
+#define RR_LD_LINEAR 1
+#define RR_LD_QUADRATIC 2
+#define RR_LD_QUADRATIC_TRI 3
+#define RR_LD_NONLINEAR 4
+#define RR_LD_GENERAL 5
+#define RR_LD_SQUARE_ROOT 6
+#define RR_LD_LOGARITHMIC 7
+#define RR_LD_EXPONENTIAL 8
+#define RR_LD_POWER_2 9
+#define RR_LD_POWER_2_PM 10
+
+int rr_abi_version(void);
+const char *rr_status_string(int status);
+/* Name of the last CUDA error seen by an entry point on this host thread. */
+const char *rr_last_cuda_error(void);
+
+/* ---- model initialisation ------------------------------------------------ */
+
+/* Replaces calculate_weights_3d (pytransit/models/roadrunner/common.py:189-223).
+ * Fills W64[nk, ng, nz] (and W32, an FP32 copy, when non-NULL) from the
+ * radial grid ze[nz] (device).  Writes dk = (kmax-kmin)/nk and dg to the host
+ * pointers (the reference's definitions, including dk's 1/nk). */
+int rr_weights_3d(int nk, double kmin, double kmax, const double *ze, int nz, int ng,
+                  double *W64, float *W32, double *dk, double *dg, void *stream);
+
+/* ---- data (set_data) ----------------------------------------------------- */
+
+/* Part of TransitModel.set_data (pytransit/models/transitmodel.py:56-125) for
+ * the split-precision path: times_ff[2*i] = hi, [2*i+1] = lo with
+ * hi + lo = times[i] - t_ref to ~2^-48 relative (FP32 pair). */
+int rr_time_split(const double *times, int npt, double t_ref, float *times_ff, void *stream);
+
+/* ---- limb-darkening layer -------------------------------------------------- */
+
+/* Replaces evaluate_ld / evaluate_ldi (pytransit/models/numba/ldmodels.py:143-174)
+ * and the numerical disk integral of rrmodel.py:219-227 (laws without ldi_*):
+ * ldc[npv, npb, npar] -> ldp[npv, npb, nz] at mu[nz], istar[npv, npb]. */
+int rr_ld_tables_f64(int law, const double *ldc, int npv, int npb, int npar, const double *mu,
+                     int nz, double *ldp, double *istar, void *stream);
+/* Same in FP32 (the split-precision path's LD layer). */
+int rr_ld_tables_f32(int law, const double *ldc, int npv, int npb, int npar, const double *mu,
+                     int nz, float *ldp, float *istar, void *stream);
+
+/* ---- full RoadRunner model --------------------------------------------------- */
+
+/* Workspace for rr_full_f64 / rr_full_split. */
+size_t rr_full_f64_workspace_bytes(int npv, int npb, int ng);
+size_t rr_full_split_workspace_bytes(int npv, int npb, int nlc, int nep, int ng);
+
+/* Replaces rr_full (pytransit/models/roadrunner/model_full.py:9-100) and
+ * rr_simple (model_simple.py:12-80), all in FP64: per-pv prologue (validity,
+ * LD means, orbit, bounding box) then flux[npv, npt].  Invalid parameter
+ * vectors (a NaN or <= 1, e < 0, ldp[pv,0,0] NaN) give NaN rows. */
+int rr_full_f64(const double *times, int npt, const double *k, int nkc, const double *t0, int ldt0,
+                const double *p, const double *a, const double *inc, const double *e,
+                const double *w, int npv, int nlc, int npb, const int32_t *lcids,
+                const int32_t *pbids, const int32_t *epids, const int32_t *nsamples,
+                const double *exptimes, const double *ldp, const double *istar,
+                const double *weights, int nk, int ng, int nz, double dk, double kmin,
+                double kmax, double dg, const double *z_edges, void *workspace,
+                size_t workspace_bytes, double *flux, int ldflux, void *stream);
+
+/* Same model, split precision: FP64 orbit (Taylor coefficients, contact
+ * points) and phase reduction data per parameter vector; per point an FP32
+ * pair phase reduction (times_ff from rr_time_split with the same t_ref,
+ * t_absmax = max |times - t_ref|), FP32 z, interpolation and flux deficit,
+ * supersamples spread over warp lanes and summed with shuffles.  ldp/istar
+ * from rr_ld_tables_f32, weights = the FP32 table.  flux is FP32. */
+int rr_full_split(const float *times_ff, double t_ref, double t_absmax, int npt, const double *k,
+                  int nkc, const double *t0, int ldt0, int nep, const double *p, const double *a,
+                  const double *inc, const double *e, const double *w, int npv, int nlc, int npb,
+                  const int32_t *lcids, const int32_t *pbids, const int32_t *epids,
+                  const int32_t *nsamples, const double *exptimes, const float *ldp,
+                  const float *istar, const float *weights, int nk, int ng, int nz, double dk,
+                  double kmin, double kmax, double dg, const double *z_edges, void *workspace,
+                  size_t workspace_bytes, float *flux, int ldflux, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYTRANSIT_GB300_H */

@@ -1,0 +1,93 @@
+"""ctypes binding of the C ABI (include/pytransit_gb300.h).
+
+The CUDA library is the only compute path: if it cannot be loaded, or no CUDA
+device is present, every model call raises.  There is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import torch
+
+from . import build as _build
+
+_LIB = None
+
+_vp = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+_sz = C.c_size_t
+
+
+class RRError(RuntimeError):
+    """A non-zero status from the CUDA library."""
+
+
+def _sig(L):
+    L.rr_abi_version.restype = _i
+    L.rr_status_string.argtypes = [_i]
+    L.rr_status_string.restype = C.c_char_p
+    L.rr_last_cuda_error.restype = C.c_char_p
+    L.rr_weights_3d.argtypes = [_i, _d, _d, _vp, _i, _i, _vp, _vp, C.POINTER(_d), C.POINTER(_d), _vp]
+    L.rr_time_split.argtypes = [_vp, _i, _d, _vp, _vp]
+    for n in ("rr_ld_tables_f64", "rr_ld_tables_f32"):
+        getattr(L, n).argtypes = [_i, _vp, _i, _i, _i, _vp, _i, _vp, _vp, _vp]
+    L.rr_full_f64_workspace_bytes.argtypes = [_i, _i, _i]
+    L.rr_full_f64_workspace_bytes.restype = _sz
+    L.rr_full_split_workspace_bytes.argtypes = [_i, _i, _i, _i, _i]
+    L.rr_full_split_workspace_bytes.restype = _sz
+    L.rr_full_f64.argtypes = ([_vp, _i, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i,
+                               _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _d,
+                               _vp, _vp, _sz, _vp, _i, _vp])
+    L.rr_full_split.argtypes = ([_vp, _d, _d, _i, _vp, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _i,
+                                 _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d,
+                                 _d, _d, _vp, _vp, _sz, _vp, _i, _vp])
+    for name, args in _EXTRA_SIGNATURES.items():
+        if hasattr(L, name):
+            getattr(L, name).argtypes = args[0]
+            getattr(L, name).restype = args[1]
+
+
+# Signatures of entry points added in other translation units (name -> (argtypes, restype)).
+_EXTRA_SIGNATURES = {}
+
+
+def lib():
+    """Build (if needed) and load libpytransit_gb300.so; raise if impossible."""
+    global _LIB
+    if _LIB is None:
+        path = _build.LIB
+        if not os.path.exists(path) or _build._stale():
+            path = _build.build()
+        L = C.CDLL(path)
+        _sig(L)
+        _LIB = L
+    return _LIB
+
+
+def check(status: int, where: str = ""):
+    if status != 0:
+        L = lib()
+        msg = L.rr_status_string(status).decode()
+        if status == 4:
+            msg += f" ({L.rr_last_cuda_error().decode()})"
+        if status == 1:
+            raise ValueError(msg)
+        raise RRError(f"{where}: {msg}" if where else msg)
+
+
+def require_cuda(device=None) -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("pytransit_gb300 needs a CUDA device (GB300, sm_103a); no CPU fallback exists")
+    dev = torch.device(device if device is not None else "cuda")
+    if dev.type != "cuda":
+        raise RuntimeError(f"pytransit_gb300 runs on CUDA devices only, not {dev}")
+    return dev
+
+
+def ptr(t):
+    """Device pointer of a torch tensor (None -> NULL)."""
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def stream_ptr(device=None):
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)

@@ -1,0 +1,234 @@
+// Device-side building blocks of the RoadRunner evaluation path.
+//
+// FP64 pieces follow the reference's numba kernels operation by operation
+// (hpparvi/PyTransit 2.8.1: pytransit/models/roadrunner/common.py,
+// model_full.py, pytransit/models/numba/ldmodels.py); FP32 pieces are the
+// per-sample arithmetic of the split-precision flux kernel.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+namespace rr {
+
+constexpr double PI = 3.141592653589793238462643383279502884;
+
+// ---------------------------------------------------------------------------
+// Circle-circle intersection (common.py:6-73)
+// ---------------------------------------------------------------------------
+
+// circle_circle_intersection_area, common.py:37-49 (two-arccos form, used for
+// the weight tables only).
+__device__ inline double cci_acos(double r1, double r2, double b) {
+  if (r1 < b - r2) return 0.0;
+  if (r1 >= b + r2) return PI * r2 * r2;
+  if (b - r2 <= -r1) return PI * r1 * r1;
+  return r2 * r2 * acos((b * b + r2 * r2 - r1 * r1) / (2 * b * r2)) +
+         r1 * r1 * acos((b * b + r1 * r1 - r2 * r2) / (2 * b * r1)) -
+         0.5 * sqrt((-b + r2 + r1) * (b + r2 - r1) * (b - r2 + r1) * (b + r2 + r1));
+}
+
+// Descending sort of three lengths (tsort, common.py:6-33).
+template <typename R>
+__device__ inline void tsort(R r1, R r2, R b, R& x, R& y, R& z) {
+  if (r1 > r2) {
+    if (r1 > b) { x = r1; if (r2 > b) { y = r2; z = b; } else { y = b; z = r2; } }
+    else { x = b; y = r1; z = r2; }
+  } else {
+    if (r2 > b) { x = r2; if (r1 > b) { y = r1; z = b; } else { y = b; z = r1; } }
+    else { x = b; y = r2; z = r1; }
+  }
+}
+
+// Area of the overlap of the unit stellar disk and a planet of radius k at
+// separation z: circle_circle_intersection_area_kite(1, k, z), common.py:53-73
+// (Agol et al. 2020).  kappa0 receives the second return value.
+template <typename R>
+__device__ inline R ccia_star(R k, R z, R& kappa0) {
+  const R one = R(1);
+  const R pi = R(PI);
+  if (one + k <= z) { kappa0 = R(0); return R(0); }
+  if (fabs(one - k) < z && z <= one + k) {
+    R x, y, w;
+    tsort<R>(one, k, z, x, y, w);
+    R a_kite = R(0.5) * sqrt((x + (y + w)) * (w - (x - y)) * (w + (x - y)) * (x + (y - w)));
+    R k0 = atan2(R(2) * a_kite, (k - one) * (k + one) + z * z);
+    R k1 = atan2(R(2) * a_kite, (one - k) * (one + k) + z * z);
+    kappa0 = k0;
+    return one * one * k1 + k * k * k0 - a_kite;
+  }
+  if (z <= one - k) { kappa0 = pi; return pi * k * k; }
+  if (z <= k - one) { kappa0 = R(0); return pi; }
+  kappa0 = R(CUDART_NAN);
+  return R(CUDART_NAN);
+}
+
+// interpolate_mean_limb_darkening_s, common.py:225-233.  The reference reads
+// lda[ng] for g in [1-1e-7, 1]; the index is clamped to ng-2 here.
+__device__ inline double interp_ldm_f64(double g, double dg, const double* lda, int ng) {
+  if (g < 0.0) return CUDART_NAN;
+  if (g > 1.0) return 0.0;
+  int i = (int)floor(g / dg);
+  if (i > ng - 2) i = ng - 2;
+  double a = (g - i * dg) / dg;
+  return (1.0 - a) * lda[i] + a * lda[i + 1];
+}
+
+// ---------------------------------------------------------------------------
+// Limb-darkening laws (pytransit/models/numba/ldmodels.py:23-140)
+// ---------------------------------------------------------------------------
+
+enum LdLaw : int {
+  LD_UNIFORM = 0, LD_LINEAR = 1, LD_QUADRATIC = 2, LD_QUADRATIC_TRI = 3, LD_NONLINEAR = 4,
+  LD_GENERAL = 5, LD_SQUARE_ROOT = 6, LD_LOGARITHMIC = 7, LD_EXPONENTIAL = 8, LD_POWER_2 = 9,
+  LD_POWER_2_PM = 10, LD_NLAWS = 11
+};
+
+template <typename R>
+__device__ inline R ld_value(int law, R mu, const R* pv, int npar) {
+  const R one = R(1);
+  switch (law) {
+    case LD_UNIFORM: return one;
+    case LD_LINEAR: return one - pv[0] * (one - mu);
+    case LD_QUADRATIC: return one - pv[0] * (one - mu) - pv[1] * (one - mu) * (one - mu);
+    case LD_QUADRATIC_TRI: {
+      R a = sqrt(pv[0]), b = R(2) * pv[1];
+      R u = a * b, v = a * (one - b);
+      return one - u * (one - mu) - v * (one - mu) * (one - mu);
+    }
+    case LD_NONLINEAR:
+      return one - pv[0] * (one - sqrt(mu)) - pv[1] * (one - mu) - pv[2] * (one - pow(mu, R(1.5))) -
+             pv[3] * (one - mu * mu);
+    case LD_GENERAL: {
+      R s = R(0);
+      for (int i = 0; i < npar; ++i) s += pv[i] * (one - pow(mu, R(i + 1)));
+      return s;
+    }
+    case LD_SQUARE_ROOT: return one - pv[0] * (one - mu) - pv[1] * (one - sqrt(mu));
+    case LD_LOGARITHMIC: return one - pv[0] * (one - mu) - pv[1] * mu * log(mu);
+    case LD_EXPONENTIAL: return one - pv[0] * (one - mu) - pv[1] / (one - exp(mu));
+    case LD_POWER_2: return one - pv[0] * (one - pow(mu, pv[1]));
+    case LD_POWER_2_PM: {
+      R c = one - pv[0] + pv[1];
+      R a = log2(c / pv[1]);
+      return one - c * (one - pow(mu, a));
+    }
+  }
+  return R(CUDART_NAN);
+}
+
+// Analytic disk integral where the RoadRunner law table has one
+// (rrmodel.py:48-58); returns false for laws integrated numerically.
+template <typename R>
+__device__ inline bool ld_integral(int law, const R* pv, R& istar) {
+  const R twopi = R(2.0 * PI);
+  switch (law) {
+    case LD_UNIFORM: istar = R(PI); return true;
+    // ldmodels.py:38-39: 2*pi*1/6*(3-2u) (the reference's normalisation, kept)
+    case LD_LINEAR: istar = twopi / R(6) * (R(3) - R(2) * pv[0]); return true;
+    case LD_QUADRATIC: istar = twopi / R(12) * (R(-2) * pv[0] - pv[1] + R(6)); return true;
+    case LD_QUADRATIC_TRI: {
+      R a = sqrt(pv[0]), b = R(2) * pv[1];
+      R u = a * b, v = a * (R(1) - b);
+      istar = twopi / R(12) * (R(-2) * u - v + R(6));
+      return true;
+    }
+    case LD_POWER_2:
+      istar = twopi * (-pv[0] * pv[1] + pv[1] + R(2)) / (R(2) * pv[1] + R(4));
+      return true;
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Orbit layer: Taylor coefficients of the sky position about conjunction
+// ---------------------------------------------------------------------------
+
+// Restatement of meepmeep's solve2d(0, p, a, i, e, w) (called at
+// model_full.py:60): exact time derivatives of the Keplerian sky position at
+// conjunction (f = pi/2 - w, orbits_py.py:83-86), propagated as a Taylor jet of
+// r'' = -mu r/|r|^3.  c[0..4] are the x coefficients, c[5..9] the y ones
+// (x(t) = sum c[j] t^j, layout of gdmodel.py:441-442); sky axes as
+// taylor_z.py:62-76.
+__device__ inline void solve2d_conj(double p, double a, double inc, double e, double w, double* c) {
+  double n = 2.0 * PI / p;
+  double se = sqrt(1.0 - e * e);
+  double sf = cos(w), cf = sin(w);  // f = pi/2 - w
+  double r = a * (1.0 - e * e) / (1.0 + e * cf);
+  double vr = n * a * e * sf / se;
+  double vt = n * a * (1.0 + e * cf) / se;
+  // in-plane position/velocity with w + f = pi/2
+  double P0x = 0.0, P0y = r;
+  double P1x = -vt, P1y = vr;
+  double mu = n * n * a * a * a;
+  const double alpha = -1.5;
+  double q0 = P0x * P0x + P0y * P0y;
+  double q1 = 2.0 * (P0x * P1x + P0y * P1y);
+  double s0 = 1.0 / (q0 * sqrt(q0));
+  double P2x = -mu * s0 * P0x / 2.0, P2y = -mu * s0 * P0y / 2.0;
+  double s1 = alpha * q1 * s0 / q0;
+  double P3x = -mu * (s0 * P1x + s1 * P0x) / 6.0;
+  double P3y = -mu * (s0 * P1y + s1 * P0y) / 6.0;
+  double q2 = 2.0 * (P0x * P2x + P0y * P2y) + (P1x * P1x + P1y * P1y);
+  double s2 = ((alpha - 1.0) * q1 * s1 + 2.0 * alpha * q2 * s0) / (2.0 * q0);
+  double P4x = -mu * (s0 * P2x + s1 * P1x + s2 * P0x) / 12.0;
+  double P4y = -mu * (s0 * P2y + s1 * P1y + s2 * P0y) / 12.0;
+  double ci = cos(inc);
+  c[0] = -P0x; c[1] = -P1x; c[2] = -P2x; c[3] = -P3x; c[4] = -P4x;
+  c[5] = -ci * P0y; c[6] = -ci * P1y; c[7] = -ci * P2y; c[8] = -ci * P3y; c[9] = -ci * P4y;
+}
+
+__device__ inline double sep_c_f64(double t, const double* c) {
+  double x = c[0] + t * (c[1] + t * (c[2] + t * (c[3] + t * c[4])));
+  double y = c[5] + t * (c[6] + t * (c[7] + t * (c[8] + t * c[9])));
+  return sqrt(x * x + y * y);
+}
+
+// Contact time by bisection, as pytransit/orbits/taylor_z.py:299-328: bracket
+// [0, s*2/vx], tolerance 1e-6 d, at most 100 steps.
+__device__ inline double contact_point(double k, int point, const double* c) {
+  double s = (point == 1 || point == 2) ? -1.0 : 1.0;
+  double zt = (point == 1 || point == 4) ? 1.0 + k : 1.0 - k;
+  double t0 = 0.0;
+  double t2 = s * 2.0 / c[1];
+  double t1 = 0.5 * t2;
+  double z0 = sep_c_f64(t0, c) - zt;
+  double z1 = sep_c_f64(t1, c) - zt;
+  for (int i = 0; fabs(t2 - t0) > 1e-6 && i < 100; ++i) {
+    if (z0 * z1 < 0.0) {
+      t2 = t1;
+      t1 = 0.5 * (t0 + t1);
+      z1 = sep_c_f64(t1, c) - zt;
+    } else {
+      t0 = t1;
+      t1 = 0.5 * (t1 + t2);
+      z0 = z1;
+      z1 = sep_c_f64(t1, c) - zt;
+    }
+  }
+  return t1;
+}
+
+// ---------------------------------------------------------------------------
+// Float-float helpers (error-free transformations, Knuth / Dekker)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+
+// Horner evaluation of the FP32 Taylor coefficients and the separation.
+__device__ __forceinline__ float sep_c_f32(float t, const float* c) {
+  float x = fmaf(t, fmaf(t, fmaf(t, fmaf(t, c[4], c[3]), c[2]), c[1]), c[0]);
+  float y = fmaf(t, fmaf(t, fmaf(t, fmaf(t, c[9], c[8]), c[7]), c[6]), c[5]);
+  return sqrtf(fmaf(x, x, y * y));
+}
+
+}  // namespace rr

@@ -1,0 +1,332 @@
+"""RoadRunnerModel: drop-in for pytransit.models.RoadRunnerModel on a GB300.
+
+Same constructor keywords, ``set_data`` and ``evaluate`` as
+pytransit/models/roadrunner/rrmodel.py:47-238.  Every evaluation runs as CUDA
+kernels through the C ABI of libpytransit_gb300.so:
+
+* ``precision='fp64'`` (default): the plain all-FP64 path (rr_full_f64),
+  matching the reference to ~1e-12 in flux.
+* ``precision='split'``: FP64 orbit and phase data per parameter vector,
+  FP32-pair phase reduction and FP32 per-sample arithmetic (rr_full_split);
+  max |dF| vs FP64 is a few 1e-7.
+
+Differences from the reference, all where the reference reads out of bounds
+or garbles its input:
+
+* a 1D ``t0`` of length npv is one zero epoch per parameter vector (the
+  documented intent, rrmodel.py:187-188); a 1D ``k`` of length npv > 1 is one
+  radius ratio per vector; scalar ``a, i, e, w`` are broadcast to npv;
+* a 2D ``ldc`` is read as [npb, ncoef] and shared by all parameter vectors;
+* k in the last table cell (ik + 1 == nk) uses the exact 2D weight table;
+* the LD-table index is clamped at g in [1 - 1e-7, 1].
+"""
+from typing import Callable, List, Tuple, Union
+from warnings import warn
+
+import numpy as np
+from numpy import ndarray
+
+from . import ldmodels as _ldm
+from .ldmodel import LDModel
+from .transitmodel import TransitModel
+
+__all__ = ['RoadRunnerModel', 'create_z_grid']
+
+
+def create_z_grid(zcut: float, nin: int, nedge: int):
+    """Radial integration grid (common.py:132-149): ``nin`` bins uniform in z
+    up to ``zcut``, ``nedge`` bins uniform in mu to the limb.  z_means[0]
+    stays 0, as in the reference."""
+    mucut = np.sqrt(1.0 - zcut ** 2)
+    dz = zcut / nin
+    dmu = mucut / nedge
+    z_edges = np.zeros(nin + nedge)
+    z_means = np.zeros(nin + nedge)
+    for i in range(nin - 1):
+        z_edges[i] = (i + 1) * dz
+    for i in range(nedge + 1):
+        z_edges[-i - 1] = np.sqrt(1 - (i * dmu) ** 2)
+    for i in range(nin + nedge - 1):
+        z_means[i + 1] = 0.5 * (z_edges[i] + z_edges[i + 1])
+    return z_edges, z_means
+
+
+class RoadRunnerModel(TransitModel):
+    ldmodels = _ldm.NAMED_LAWS
+
+    def __init__(self, ldmodel: Union[str, Callable, Tuple[Callable, Callable]] = 'quadratic',
+                 precompute_weights: bool = False, klims: tuple = (0.005, 0.5), nk: int = 256,
+                 nzin: int = 20, nzlimb: int = 20, zcut: float = 0.7, ng: int = 100,
+                 nthreads: int = 1, small_planet_limit: float = 0.05, precision: str = 'fp64',
+                 device=None, **kwargs):
+        """The RoadRunner transit model by Parviainen (2020), on the GPU.
+
+        Parameters
+        ----------
+        ldmodel : str, callable, (callable, callable) or LDModel
+            A named law (``RoadRunnerModel.ldmodels``), a profile callable
+            ``I(mu, pv)`` (disk integral by a 200-point trapezoid), a
+            (profile, integral) tuple, or an LDModel instance.
+        precompute_weights : bool
+            Kept for the transmission-spectroscopy model; the 3D weight table is
+            always used here, as in the reference.
+        klims, nk : radius-ratio range and grid size of the weight table.
+        nzin, nzlimb, zcut : radial grid (inner disk, limb, their boundary).
+        ng : size of the grazing-parameter grid.
+        nthreads, small_planet_limit : accepted for compatibility; unused.
+        precision : 'fp64' (plain FP64 path) or 'split' (FP32 per-sample path).
+        device : CUDA device (default: the current one).
+        """
+        super().__init__()
+        if 'interpolate' in kwargs:
+            warn("The 'interpolate' argument has been replaced by 'precompute_weights' and will be removed in the future.", FutureWarning)
+            self.interpolate: bool = kwargs.get('interpolate', False)
+        else:
+            self.interpolate: bool = precompute_weights
+        if 'parallel' in kwargs:
+            warn("The 'parallel' argument has been replaced by 'nthreads' and will be removed in the future.", FutureWarning)
+        self.nthreads = nthreads
+        self.splimit = small_planet_limit
+        if precision not in ('fp64', 'split'):
+            raise ValueError("precision must be 'fp64' or 'split'")
+        self.precision = precision
+        self.device = device
+
+        # Limb darkening model (rrmodel.py:109-131)
+        self.ld_law = None           # device law id of a named law, else None
+        if isinstance(ldmodel, str):
+            try:
+                entry = self.ldmodels[ldmodel]
+            except KeyError:
+                print(f"Unknown limb darkening model: {ldmodel}. Choose from [{', '.join(self.ldmodels.keys())}] or supply a callable function.")
+                raise
+            self.ldmodel, self.ldmmean = entry if isinstance(entry, tuple) else (entry, None)
+            self.ld_law = _ldm.LAW_IDS[ldmodel]
+        elif isinstance(ldmodel, LDModel):
+            self.ldmodel = ldmodel
+            self.ldmmean = ldmodel._integrate
+        elif callable(ldmodel):
+            self.ldmodel = ldmodel
+            self.ldmmean = None
+        elif isinstance(ldmodel, tuple) and callable(ldmodel[0]) and callable(ldmodel[1]):
+            self.ldmodel, self.ldmmean = ldmodel
+        else:
+            raise NotImplementedError
+        if self.ld_law is None:
+            # the library's own law functions still run on the device
+            for name, entry in self.ldmodels.items():
+                fl, fi = entry if isinstance(entry, tuple) else (entry, None)
+                if self.ldmodel is fl and self.ldmmean is fi:
+                    self.ld_law = _ldm.LAW_IDS[name]
+
+        self.klims = klims
+        self.nk, self.ng, self.nzin, self.nzlimb, self.zcut = nk, ng, nzin, nzlimb, zcut
+        self._ldmu = np.linspace(1, 0, 200)
+        self._ldz = np.sqrt(1 - self._ldmu ** 2)
+        self._tables = None
+        self._ws = None
+        self.init_integration(nzin, nzlimb, zcut, ng, nk)
+
+    # ------------------------------------------------------------------
+    def init_integration(self, nzin, nzlimb, zcut, ng, nk):
+        """Integration grid and weight-table constants (rrmodel.py:165-173);
+        the table itself is built on the GPU at first use."""
+        self.nk, self.ng, self.nzin, self.nzlimb, self.zcut = nk, ng, nzin, nzlimb, zcut
+        self.ze, self.zm = create_z_grid(zcut, nzin, nzlimb)
+        self.mu = np.sqrt(1 - self.zm ** 2)
+        self.dk = (self.klims[1] - self.klims[0]) / nk
+        self.dg = (1.0 - 1e-7) / (ng - 1)
+        self._tables = None
+
+    def set_data(self, time, lcids=None, pbids=None, nsamples=None, exptimes=None, epids=None) -> None:
+        super().set_data(time, lcids, pbids, nsamples, exptimes, epids)
+        self.nep = np.unique(self.epids).size
+
+    # ------------------------------------------------------------------
+    def _cuda_device(self):
+        from . import _lib
+        return _lib.require_cuda(self.device)
+
+    def _device_tables(self, device):
+        """Weight table W[nk, ng, nz] (FP64 and FP32) and the grids, on the GPU."""
+        import ctypes as C
+        import torch
+        from . import _lib
+        if self._tables is not None and self._tables['device'] == device:
+            return self._tables
+        nz = self.ze.size
+        t = {'device': device}
+        t['ze'] = torch.as_tensor(self.ze, dtype=torch.float64).to(device)
+        t['mu'] = torch.as_tensor(self.mu, dtype=torch.float64).to(device)
+        t['W64'] = torch.empty((self.nk, self.ng, nz), dtype=torch.float64, device=device)
+        t['W32'] = torch.empty((self.nk, self.ng, nz), dtype=torch.float32, device=device)
+        dk, dg = C.c_double(), C.c_double()
+        _lib.check(_lib.lib().rr_weights_3d(self.nk, float(self.klims[0]), float(self.klims[1]),
+                                            _lib.ptr(t['ze']), nz, self.ng, _lib.ptr(t['W64']),
+                                            _lib.ptr(t['W32']), C.byref(dk), C.byref(dg),
+                                            _lib.stream_ptr(device)), "rr_weights_3d")
+        self.dk, self.dg = dk.value, dg.value
+        self._tables = t
+        return t
+
+    def _workspace(self, nbytes, device):
+        import torch
+        if self._ws is None or self._ws.numel() < nbytes or self._ws.device != device:
+            self._ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device)
+        return self._ws
+
+    # ------------------------------------------------------------------
+    @staticmethod
+    def _vec(x, npv, name):
+        x = np.atleast_1d(np.asarray(x, dtype=np.float64))
+        if x.size == 1 and npv > 1:
+            x = np.full(npv, x.reshape(-1)[0])
+        if x.ndim != 1 or x.size != npv:
+            raise ValueError(f"'{name}' should be a scalar or a vector of {npv} values.")
+        return np.ascontiguousarray(x)
+
+    def _shape_params(self, k, t0, p, a, i, e, w):
+        """Parameter arrays shaped as rr_full expects (rrmodel.py:229-230)."""
+        p = np.atleast_1d(np.asarray(p, dtype=np.float64))
+        npv = p.size
+        k = np.asarray(k, dtype=np.float64)
+        if k.ndim == 0:
+            k = k.reshape(1, 1)
+        elif k.ndim == 1:
+            k = k.reshape(npv, 1) if (npv > 1 and k.size == npv) else k.reshape(1, -1)
+        if k.shape[0] == 1 and npv > 1:
+            k = np.repeat(k, npv, axis=0)
+        if k.shape[0] != npv:
+            raise ValueError(f"Radius ratios given for {k.shape[0]} parameter vectors, expected {npv}.")
+        if k.shape[1] > 1 and k.shape[1] != self.npb:
+            raise ValueError('Radius ratios should be given either as an [npv, 1] or [npv, npb] array.')
+        t0 = np.asarray(t0, dtype=np.float64)
+        if t0.ndim == 0:
+            t0 = np.full((npv, 1), float(t0))
+        elif t0.ndim == 1:
+            t0 = t0.reshape(npv, 1) if t0.size == npv else np.tile(t0, (npv, 1))
+        elif t0.shape[0] == 1 and npv > 1:
+            t0 = np.repeat(t0, npv, axis=0)
+        if t0.shape[0] != npv:
+            raise ValueError(f"Zero epochs given for {t0.shape[0]} parameter vectors, expected {npv}.")
+        eps = np.asarray(self.epids).reshape(-1)
+        if eps.size and eps.max() >= t0.shape[1]:
+            raise ValueError(f"Epoch index {eps.max()} needs a zero epoch array with at least {eps.max() + 1} columns.")
+        a, i, e, w = (self._vec(x, npv, n) for x, n in ((a, 'a'), (i, 'i'), (e, 'e'), (w, 'w')))
+        return (np.ascontiguousarray(k), np.ascontiguousarray(t0), np.ascontiguousarray(p), a, i, e, w)
+
+    def _shape_ldc(self, ldc, npv, npb):
+        ldc = np.asarray(ldc, dtype=np.float64)
+        if ldc.ndim == 0:
+            ldc = ldc.reshape(1, 1, 1)
+        elif ldc.ndim == 1:
+            ldc = ldc.reshape(1, 1, -1)
+        elif ldc.ndim == 2:
+            ldc = ldc.reshape(1, ldc.shape[0], -1)
+        if ldc.shape[1] == 1 and npb > 1:
+            ldc = np.repeat(ldc, npb, axis=1)
+        if ldc.shape[0] == 1 and npv > 1:
+            ldc = np.repeat(ldc, npv, axis=0)
+        if ldc.shape[0] != npv or ldc.shape[1] != npb:
+            raise ValueError(f"Limb darkening coefficients should be given as a [npv, npb, ncoef] array "
+                             f"with npv={npv}, npb={npb}; got {ldc.shape}.")
+        return np.ascontiguousarray(ldc)
+
+    def _ld_tables(self, ldc, npv, npb, device, split):
+        """(ldp[npv, npb, nz], istar[npv, npb]) on the device (rrmodel.py:212-227)."""
+        import torch
+        from . import _lib
+        tb = self._device_tables(device)
+        nz = self.ze.size
+        dt = torch.float32 if split else torch.float64
+        if self.ld_law is not None:
+            ldc3 = self._shape_ldc(ldc, npv, npb)
+            ldc_d = torch.as_tensor(ldc3).to(device)
+            ldp = torch.empty((npv, npb, nz), dtype=dt, device=device)
+            istar = torch.empty((npv, npb), dtype=dt, device=device)
+            fn = _lib.lib().rr_ld_tables_f32 if split else _lib.lib().rr_ld_tables_f64
+            _lib.check(fn(self.ld_law, _lib.ptr(ldc_d), npv, npb, ldc3.shape[2], _lib.ptr(tb['mu']), nz,
+                          _lib.ptr(ldp), _lib.ptr(istar), _lib.stream_ptr(device)), "rr_ld_tables")
+            return ldp, istar
+        # host LD models: evaluated on the CPU, uploaded
+        if isinstance(self.ldmodel, LDModel):
+            ldp, istar = self.ldmodel(self.mu, np.atleast_1d(np.asarray(ldc, dtype=np.float64)))
+        else:
+            ldc3 = self._shape_ldc(ldc, npv, npb)
+            ldp = _ldm.evaluate_ld(self.ldmodel, self.mu, ldc3)
+            if self.ldmmean is not None:
+                istar = _ldm.evaluate_ldi(self.ldmmean, ldc3)
+            else:
+                ldpi = _ldm.evaluate_ld(self.ldmodel, self._ldmu, ldc3)
+                istar = 2 * np.pi * np.trapezoid(self._ldz * ldpi, self._ldz, axis=-1)
+        ldp = np.asarray(ldp, dtype=np.float64)
+        ldp = ldp.reshape((1,) * (3 - ldp.ndim) + ldp.shape) if ldp.ndim < 3 else ldp
+        istar = np.asarray(istar, dtype=np.float64)
+        istar = istar.reshape((1,) * (2 - istar.ndim) + istar.shape) if istar.ndim < 2 else istar
+        try:
+            ldp = np.broadcast_to(ldp, (npv, npb, nz))
+            istar = np.broadcast_to(istar, (npv, npb))
+        except ValueError:
+            raise ValueError(f"The limb darkening model returned ldp {ldp.shape} and istar {istar.shape}; "
+                             f"expected [{npv}, {npb}, {nz}] and [{npv}, {npb}].") from None
+        ldp_d = torch.as_tensor(np.ascontiguousarray(ldp)).to(device=device, dtype=dt)
+        istar_d = torch.as_tensor(np.ascontiguousarray(istar)).to(device=device, dtype=dt)
+        return ldp_d, istar_d
+
+    # ------------------------------------------------------------------
+    def evaluate(self, k: Union[float, ndarray], ldc: Union[ndarray, List], t0: Union[float, ndarray],
+                 p: Union[float, ndarray], a: Union[float, ndarray], i: Union[float, ndarray],
+                 e: Union[float, ndarray] = 0.0, w: Union[float, ndarray] = 0.0, copy: bool = True):
+        """Evaluate the transit model for one or many parameter vectors.
+
+        Returns the modelled flux, [npt] for one parameter vector and
+        [npv, npt] for many (squeezed as the reference does).  With copy=True a
+        float64 numpy array; with copy=False the torch tensor on the GPU
+        (float64, or float32 in the split precision)."""
+        import torch
+        from . import _lib
+        device = self._cuda_device()
+        k, t0, p, a, i, e, w = self._shape_params(k, t0, p, a, i, e, w)
+        npv, npt, npb, nlc = p.size, self.npt, self.npb, self.nlc
+        split = self.precision == 'split'
+        tb = self._device_tables(device)
+        dd = self._device_data(device)
+        ldp, istar = self._ld_tables(ldc, npv, npb, device, split)
+        args = {n: torch.as_tensor(v).to(device) for n, v in
+                dict(k=k, t0=t0, p=p, a=a, i=i, e=e, w=w).items()}
+        L = _lib.lib()
+        stream = _lib.stream_ptr(device)
+        nz = self.ze.size
+        if split:
+            ldf = (npt + 3) // 4 * 4
+            out = torch.empty((npv, ldf), dtype=torch.float32, device=device)
+            nep = t0.shape[1]
+            wsb = L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, self.ng)
+            ws = self._workspace(wsb, device)
+            st = L.rr_full_split(_lib.ptr(dd['times_ff']), dd['t_ref'], dd['t_absmax'], npt,
+                                 _lib.ptr(args['k']), k.shape[1], _lib.ptr(args['t0']), t0.shape[1], nep,
+                                 _lib.ptr(args['p']), _lib.ptr(args['a']), _lib.ptr(args['i']),
+                                 _lib.ptr(args['e']), _lib.ptr(args['w']), npv, nlc, npb,
+                                 _lib.ptr(dd['lcids']), _lib.ptr(dd['pbids']), _lib.ptr(dd['epids']),
+                                 _lib.ptr(dd['nsamples']), _lib.ptr(dd['exptimes']), _lib.ptr(ldp),
+                                 _lib.ptr(istar), _lib.ptr(tb['W32']), self.nk, self.ng, nz, self.dk,
+                                 float(self.klims[0]), float(self.klims[1]), self.dg, _lib.ptr(tb['ze']),
+                                 _lib.ptr(ws), ws.numel(), _lib.ptr(out), ldf, stream)
+            out = out[:, :npt]
+        else:
+            out = torch.empty((npv, npt), dtype=torch.float64, device=device)
+            wsb = L.rr_full_f64_workspace_bytes(npv, npb, self.ng)
+            ws = self._workspace(wsb, device)
+            st = L.rr_full_f64(_lib.ptr(dd['time']), npt, _lib.ptr(args['k']), k.shape[1],
+                               _lib.ptr(args['t0']), t0.shape[1], _lib.ptr(args['p']), _lib.ptr(args['a']),
+                               _lib.ptr(args['i']), _lib.ptr(args['e']), _lib.ptr(args['w']), npv, nlc, npb,
+                               _lib.ptr(dd['lcids']), _lib.ptr(dd['pbids']), _lib.ptr(dd['epids']),
+                               _lib.ptr(dd['nsamples']), _lib.ptr(dd['exptimes']), _lib.ptr(ldp),
+                               _lib.ptr(istar), _lib.ptr(tb['W64']), self.nk, self.ng, nz, self.dk,
+                               float(self.klims[0]), float(self.klims[1]), self.dg, _lib.ptr(tb['ze']),
+                               _lib.ptr(ws), ws.numel(), _lib.ptr(out), npt, stream)
+        _lib.check(st, "rr_full")
+        out = out.squeeze()
+        if copy:
+            return out.to(torch.float64).cpu().numpy()
+        return out

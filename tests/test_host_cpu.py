@@ -1,0 +1,135 @@
+"""CPU-only tests: the C ABI library loads and exports every declared symbol,
+and the host-side logic of the drop-in (set_data validation, parameter
+shaping, LD-model resolution) behaves as the reference's."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "pytransit_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(rr_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    from pytransit_gb300 import build
+    path = build.build()
+    L = ctypes.CDLL(path)
+    names = declared_functions()
+    assert len(names) >= 10
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_status_strings_and_workspace_sizes():
+    from pytransit_gb300 import _lib
+    L = _lib.lib()
+    assert L.rr_abi_version() >= 1
+    assert L.rr_status_string(0) == b"ok"
+    assert b"npv, npb" in L.rr_status_string(1)
+    assert L.rr_full_f64_workspace_bytes(10, 4, 100) >= 10 * 16 * 8 + 10 * 4 * 100 * 8
+    assert L.rr_full_split_workspace_bytes(10, 4, 4, 1, 100) >= 10 * 4 * 100 * 4
+
+
+def test_argument_errors_without_gpu():
+    """Argument checks return before any launch, so they run without a GPU."""
+    from pytransit_gb300 import _lib
+    L = _lib.lib()
+    # k with 3 columns and 4 passbands -> RR_ERR_SHAPE
+    st = L.rr_full_f64(None, 10, None, 3, None, 1, None, None, None, None, None, 2, 1, 4, None, None, None,
+                       None, None, None, None, None, 256, 100, 40, 0.1, 0.005, 0.5, 0.01, None, None, 0,
+                       None, 10, None)
+    assert st == 1
+    # unknown law id
+    assert L.rr_ld_tables_f64(99, None, 1, 1, 2, None, 40, None, None, None) == 5
+    # ldflux < npt
+    st = L.rr_full_f64(None, 10, None, 1, None, 1, None, None, None, None, None, 2, 1, 1, None, None, None,
+                       None, None, None, None, None, 256, 100, 40, 0.1, 0.005, 0.5, 0.01, None, None, 0,
+                       None, 5, None)
+    assert st == 2
+    # workspace too small
+    st = L.rr_full_f64(None, 10, None, 1, None, 1, None, None, None, None, None, 2, 1, 1, None, None, None,
+                       None, None, None, None, None, 256, 100, 40, 0.1, 0.005, 0.5, 0.01, None, None, 16,
+                       None, 10, None)
+    assert st == 3
+
+
+def test_z_grid_matches_oracle():
+    import oracle
+    from pytransit_gb300 import create_z_grid
+    ze, zm = create_z_grid(0.7, 20, 20)
+    oze, ozm = oracle.z_grid(0.7, 20, 20)
+    np.testing.assert_array_equal(ze, oze)
+    np.testing.assert_array_equal(zm, ozm)
+
+
+def test_set_data_validation_mirrors_reference():
+    from pytransit_gb300 import RoadRunnerModel
+    m = RoadRunnerModel('quadratic')
+    t = np.linspace(0, 1, 10)
+    with pytest.raises(ValueError, match="must be given as integers"):
+        m.set_data(t, lcids=np.zeros(10))
+    with pytest.raises(ValueError, match="should equal to the number of datapoints"):
+        m.set_data(t, lcids=np.zeros(9, int))
+    with pytest.raises(ValueError, match="should equal to the number of ligt curves"):
+        m.set_data(t, lcids=np.zeros(10, int), pbids=[0, 1])
+    with pytest.raises(ValueError, match="between 0 and"):
+        m.set_data(t, lcids=np.repeat([0, 1], 5), pbids=[0, 2])
+    with pytest.raises(ValueError):
+        m.set_data(np.array([]))          # the reference fails on empty data as well
+    m.set_data(t, lcids=np.repeat([0, 1], 5), pbids=[0, 1], nsamples=[1, 5], exptimes=[0, 0.01])
+    assert (m.nlc, m.npb, m.npt) == (2, 2, 10)
+    # same time object, no other args: no-op (transitmodel.py:83-84)
+    m.set_data(t)
+    assert m.nlc == 2
+
+
+def test_ld_model_resolution():
+    from pytransit_gb300 import LDModel, RoadRunnerModel, ldmodels
+    assert RoadRunnerModel('power-2').ld_law == 9
+    assert RoadRunnerModel((ldmodels.ld_quadratic, ldmodels.ldi_quadratic)).ld_law == 2
+    assert RoadRunnerModel(lambda mu, pv: 1 - pv[0] * (1 - mu)).ld_law is None
+    with pytest.raises(KeyError):
+        RoadRunnerModel('no-such-law')
+    with pytest.raises(NotImplementedError):
+        RoadRunnerModel(42)
+
+    class L(LDModel):
+        def _evaluate(self, mu, x):
+            return np.ones(np.shape(x)[:-1] + (np.size(mu),))
+    m = RoadRunnerModel(L())
+    assert m.ld_law is None and m.ldmmean is not None
+    assert abs(L()._integrate(np.zeros((2, 3, 1)))[1, 2] - np.pi) < 1e-4
+
+
+def test_parameter_shaping():
+    from pytransit_gb300 import RoadRunnerModel
+    m = RoadRunnerModel('quadratic')
+    m.set_data(np.linspace(0, 1, 10), lcids=np.repeat([0, 1], 5), pbids=[0, 1], epids=[0, 1])
+    k, t0, p, a, i, e, w = m._shape_params([0.1, 0.11, 0.12], [[0.0, 0.01]], [1, 2, 3], 5.0, 1.5, 0.0, 0.0)
+    assert k.shape == (3, 1) and t0.shape == (3, 2) and a.shape == (3,)
+    with pytest.raises(ValueError, match="npv, 1"):
+        m._shape_params(np.ones((3, 3)), [[0.0, 0.01]], [1, 2, 3], 5.0, 1.5, 0.0, 0.0)
+    with pytest.raises(ValueError, match="Epoch index"):
+        m._shape_params(0.1, 0.0, 1.0, 5.0, 1.5, 0.0, 0.0)
+    assert m._shape_ldc([0.3, 0.1], 3, 2).shape == (3, 2, 2)
+    assert m._shape_ldc(np.ones((2, 2)), 3, 2).shape == (3, 2, 2)
+    with pytest.raises(ValueError):
+        m._shape_ldc(np.ones((3, 3, 2)), 3, 2)
+
+
+def test_no_cpu_fallback():
+    import torch
+    from pytransit_gb300 import RoadRunnerModel
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    m = RoadRunnerModel('quadratic')
+    m.set_data(np.linspace(-0.1, 0.1, 10))
+    with pytest.raises(RuntimeError, match="CUDA"):
+        m.evaluate(0.1, [0.3, 0.1], 0.0, 2.0, 7.0, 1.55)

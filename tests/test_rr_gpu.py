@@ -1,0 +1,213 @@
+"""GPU parity of the RoadRunner path (plain FP64 and split precision) against
+the golden fixtures made by the reference's own code and against the oracle.
+
+Tolerances (max |dF|, absolute flux):
+  * FP64 path vs reference / oracle: 1e-9
+  * split path vs reference / oracle / FP64 path: 1e-6
+NaN rows and points must match exactly.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = {'fp64': 1e-9, 'split': 1e-6}
+
+
+def rr(law='quadratic', precision='fp64', **kw):
+    from pytransit_gb300 import RoadRunnerModel
+    return RoadRunnerModel(law, precision=precision, **kw)
+
+
+def max_err(got, want):
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    assert got.shape == want.shape, (got.shape, want.shape)
+    assert np.array_equal(np.isnan(got), np.isnan(want)), "NaN pattern differs"
+    m = ~np.isnan(want)
+    return float(np.abs(got[m] - want[m]).max()) if m.any() else 0.0
+
+
+def pv_args(g):
+    return g["k"], g["ldc"], g["t0"], g["p"], g["a"], g["inc"], g["e"], g["w"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_golden_c0(golden, precision):
+    g = golden("c0_quadratic")
+    m = rr(precision=precision)
+    m.set_data(g["time"])
+    assert max_err(m.evaluate(*pv_args(g)), g["flux"]) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_golden_multi_lc_bjd(golden, precision):
+    g = golden("multi_lc_bjd")
+    m = rr(precision=precision)
+    m.set_data(g["time"], lcids=g["lcids"], pbids=g["pbids"], nsamples=g["nsamples"],
+               exptimes=g["exptimes"], epids=g["epids"])
+    assert max_err(m.evaluate(*pv_args(g)), g["flux"]) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_golden_power2_supersampled(golden, precision):
+    g = golden("power2_ss10")
+    m = rr('power-2', precision=precision)
+    m.set_data(g["time"], lcids=g["lcids"], pbids=g["pbids"], nsamples=g["nsamples"], exptimes=g["exptimes"])
+    assert max_err(m.evaluate(*pv_args(g)), g["flux"]) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("law", list(oracle.LD_LAWS))
+def test_golden_ld_laws(golden, law, precision):
+    g = golden("ld_laws")
+    m = rr(law, precision=precision)
+    m.set_data(g["time"])
+    flux = m.evaluate(g["k"], g[f"ldc__{law}"], g["t0"], g["p"], g["a"], g["inc"], g["e"], g["w"])
+    assert max_err(flux, g[f"flux__{law}"]) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_golden_user_ld(golden, precision):
+    from pytransit_gb300 import LDModel, ldmodels
+
+    g = golden("user_ld")
+
+    class QuadLD(LDModel):
+        def _evaluate(self, mu, x):
+            x = np.asarray(x)
+            return 1.0 - x[..., 0:1] * (1.0 - mu) - x[..., 1:2] * (1.0 - mu) ** 2
+
+        def _integrate(self, x):
+            x = np.asarray(x)
+            return 2 * np.pi / 12 * (-2 * x[..., 0] - x[..., 1] + 6)
+
+    def user_law(mu, pv):
+        return 1.0 - pv[0] * (1.0 - mu) - pv[1] * (1.0 - np.sqrt(mu))
+
+    for name, model in [("ldmodel", QuadLD()), ("callable", user_law),
+                        ("tuple", (ldmodels.ld_quadratic, ldmodels.ldi_quadratic))]:
+        m = rr(model, precision=precision)
+        m.set_data(g["time"])
+        assert max_err(m.evaluate(*pv_args(g)), g[f"flux__{name}"]) <= TOL[precision], name
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_golden_klims(golden, precision):
+    g = golden("klims")
+    m = rr(precision=precision)
+    m.set_data(g["time"])
+    assert max_err(m.evaluate(*pv_args(g)), g["flux"]) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_golden_simple(golden, precision):
+    g = golden("simple")
+    m = rr(precision=precision)
+    m.set_data(g["time"], nsamples=[4], exptimes=[0.01])
+    flux = m.evaluate(float(g["k"]), g["ldc"], float(g["t0"]), float(g["p"]), float(g["a"]),
+                      float(g["inc"]), float(g["e"]), float(g["w"]))
+    assert flux.shape == g["flux"].shape
+    assert max_err(flux, g["flux"]) <= TOL[precision]
+
+
+def c1_like(rng, npv, npt, nlc=4, T=2459000.0, cadence=2 / 1440, ns=1, exptime=0.0, ecc=False,
+            p_range=(0.5, 15.0)):
+    """Contiguous light curves (one passband each) at BJD scale."""
+    time = T + np.arange(npt) * cadence
+    lcids = np.minimum((np.arange(npt) * nlc) // npt, nlc - 1)
+    k = rng.uniform(0.05, 0.15, (npv, 1))
+    ldc = np.stack([rng.uniform(0, .6, (npv, nlc)), rng.uniform(0, .3, (npv, nlc))], -1)
+    t0 = T + rng.normal(0, 1e-3, (npv, 1))
+    p = rng.uniform(*p_range, npv)
+    a = rng.uniform(3, 20, npv)
+    inc = np.arccos(rng.uniform(0, .9, npv) / a)
+    e = rng.uniform(0, .3, npv) if ecc else np.zeros(npv)
+    w = rng.uniform(0, 2 * np.pi, npv) if ecc else np.zeros(npv)
+    data = dict(time=time, lcids=lcids, pbids=np.arange(nlc), nsamples=np.full(nlc, ns),
+                exptimes=np.full(nlc, exptime))
+    return data, (k, ldc, t0, p, a, inc, e, w)
+
+
+@pytest.mark.parametrize("ns,exptime,ecc", [(1, 0.0, False), (10, 1 / 48, True), (3, 0.02, True)])
+def test_oracle_parity_bjd(ns, exptime, ecc):
+    """FP64 and split paths vs the oracle on a 96 x 19,700 BJD-scale workload
+    (2-min cadence over 27.4 d, four light curves / passbands)."""
+    rng = np.random.default_rng(100 + ns)
+    data, args = c1_like(rng, 96, 19700, ns=ns, exptime=exptime, ecc=ecc)
+    ref = oracle.OracleRoadRunner('quadratic')
+    ref.set_data(**data)
+    want = ref.evaluate(*args)
+    for precision in ("fp64", "split"):
+        m = rr(precision=precision)
+        m.set_data(**data)
+        err = max_err(m.evaluate(*args), want)
+        assert err <= TOL[precision], (precision, err)
+
+
+def test_split_vs_fp64_long_baseline():
+    """Split vs FP64 over a 1000-day baseline at 30-min cadence with 10
+    supersamples, power-2 LD, eccentric orbits (the precision workload's shape)."""
+    rng = np.random.default_rng(7)
+    npv = 512
+    npts = np.exp(rng.uniform(np.log(500), np.log(50000), 16)).astype(int)
+    time = np.concatenate([2459000.0 + np.arange(n) / 48.0 for n in npts])
+    lcids = np.concatenate([np.full(n, j) for j, n in enumerate(npts)])
+    data = dict(time=time, lcids=lcids, pbids=np.arange(16) % 4, nsamples=np.full(16, 10),
+                exptimes=np.full(16, 1 / 48))
+    k = rng.uniform(0.05, 0.15, (npv, 1))
+    ldc = np.stack([rng.uniform(.3, .9, (npv, 4)), rng.uniform(.3, .8, (npv, 4))], -1)
+    t0 = 2459000.0 + rng.normal(0, 1e-3, (npv, 1))
+    p = rng.uniform(0.5, 15, npv)
+    a = rng.uniform(3, 20, npv)
+    inc = np.arccos(rng.uniform(0, .9, npv) / a)
+    e = rng.uniform(0, .3, npv)
+    w = rng.uniform(0, 2 * np.pi, npv)
+    out = {}
+    for precision in ("fp64", "split"):
+        m = rr('power-2', precision=precision)
+        m.set_data(**data)
+        out[precision] = m.evaluate(k, ldc, t0, p, a, inc, e, w)
+    assert max_err(out["split"], out["fp64"]) <= 1e-6
+    assert np.sum(out["fp64"] < 1) > 1000   # the case does exercise in-transit points
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("npt", [1, 2, 5, 127, 129, 1023, 1025])
+def test_ragged_sizes(precision, npt):
+    rng = np.random.default_rng(npt)
+    time = np.linspace(-0.1, 0.1, npt)
+    npv = 3
+    args = (rng.uniform(0.08, 0.12, (npv, 1)), np.tile([0.3, 0.1], (npv, 1, 1)), np.zeros((npv, 1)),
+            np.full(npv, 2.0), np.full(npv, 7.0), np.full(npv, np.arccos(0.2 / 7)), np.zeros(npv),
+            np.zeros(npv))
+    ref = oracle.OracleRoadRunner('quadratic')
+    ref.set_data(time)
+    m = rr(precision=precision)
+    m.set_data(time)
+    assert max_err(m.evaluate(*args), ref.evaluate(*args)) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_invalid_rows_are_nan(precision):
+    time = np.linspace(-0.1, 0.1, 200)
+    npv = 4
+    m = rr(precision=precision)
+    m.set_data(time)
+    a = np.array([5.0, 0.9, np.nan, 5.0])
+    e = np.array([0.0, 0.0, 0.0, -0.1])
+    flux = m.evaluate(np.full((npv, 1), 0.1), np.tile([0.3, 0.1], (npv, 1, 1)), np.zeros((npv, 1)),
+                      np.full(npv, 2.0), a, np.full(npv, 1.55), e, np.zeros(npv))
+    assert np.all(np.isfinite(flux[0]))
+    assert np.all(np.isnan(flux[1:]))
+
+
+def test_device_output_and_copy_false():
+    import torch
+    time = np.linspace(-0.1, 0.1, 100)
+    m = rr(precision='split')
+    m.set_data(time)
+    out = m.evaluate(np.array([[0.1], [0.11]]), [0.3, 0.1], [0.0, 0.0], [2.0, 2.1], 7.0, 1.55, copy=False)
+    assert isinstance(out, torch.Tensor) and out.is_cuda and out.shape == (2, 100)
+    assert out.dtype == torch.float32
