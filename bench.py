@@ -1,0 +1,399 @@
+#!/usr/bin/env python
+"""RoadRunner transit-model throughput on GB300.
+
+Workload (one "step" = one evaluation of the model for a whole population):
+8192 parameter vectors x 19,700 times (2-min cadence over 27.4 d at BJD
+2459000), four contiguous light curves in four passbands, quadratic limb
+darkening, nsamples = 1; k ~ U(0.05, 0.15), t0 ~ 2459000 + N(0, 1e-3),
+p ~ U(0.5, 15), a ~ U(3, 20), b ~ U(0, 0.9), e = w = 0; seeded synthetic data.
+
+Reported (one JSON line from rank 0):
+  value      model points/s of the split-precision path, inputs resident in HBM
+             (LD tables + prologue + flux kernels per step, CUDA events);
+  e2e        the same through the public API (RoadRunnerModel.evaluate) with
+             host parameter arrays in and the flux copied to pinned host memory;
+  fp64       the plain all-FP64 GPU path on the same inputs;
+  roofline   the flux kernel's algorithmic bytes / its event-timed duration
+             against the measured HBM copy bandwidth;
+  cpu_baseline  the oracle's FP64 C port (OpenMP, all host cores) on a
+             bounded sample of the same workload.
+``--impl reference`` times that CPU implementation alone (the reference's
+path restated in C; the reference itself is Python + numba, absent here).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = ("8192 parameter vectors x 19700 times (2-min cadence, 27.4 d, BJD 2459000), "
+            "4 light curves / passbands, quadratic LD, nsamples=1")
+METRIC = "model points/s (RoadRunner flux values per second)"
+
+
+def workload(npv=8192, npt=19700, seed=1234):
+    rng = np.random.default_rng(seed)
+    T = 2459000.0
+    nlc = 4
+    time_ = T + np.arange(npt) * (2.0 / 1440.0)
+    lcids = np.minimum((np.arange(npt) * nlc) // npt, nlc - 1).astype(np.int64)
+    k = rng.uniform(0.05, 0.15, (npv, 1))
+    ldc = np.stack([rng.uniform(0, .6, (npv, nlc)), rng.uniform(0, .3, (npv, nlc))], -1)
+    t0 = T + rng.normal(0, 1e-3, (npv, 1))
+    p = rng.uniform(0.5, 15.0, npv)
+    a = rng.uniform(3.0, 20.0, npv)
+    inc = np.arccos(rng.uniform(0.0, 0.9, npv) / a)
+    e = np.zeros(npv)
+    w = np.zeros(npv)
+    data = dict(time=time_, lcids=lcids, pbids=np.arange(nlc), nsamples=np.ones(nlc, int),
+                exptimes=np.zeros(nlc))
+    return data, dict(k=k, ldc=ldc, t0=t0, p=p, a=a, i=inc, e=e, w=w)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(npv, npt):
+    """DRAM bytes per launch of the split flux kernel from the committed ncu
+    summary (profiles/flux_split_c1.md), scaled to this launch's points."""
+    path = os.path.join(ROOT, "profiles", "flux_split_c1.md")
+    if not os.path.exists(path):
+        return None
+    vals = {}
+    with open(path) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_point:"):
+                vals["bpp"] = float(line.split(":")[1])
+    if "bpp" not in vals:
+        return None
+    return vals["bpp"] * npv * npt
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 8:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in rows for j in range(4) if r[4 + j].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_rr_full(model, prm, npv_sample, nthreads):
+    import oracle
+    ldp, istar = oracle.evaluate_ld_named('quadratic', model.mu, prm["ldc"][:npv_sample])
+    sl = slice(0, npv_sample)
+    return oracle.rr_full(model.time, prm["k"][sl], prm["t0"][sl], prm["p"][sl], prm["a"][sl], prm["i"][sl],
+                          prm["e"][sl], prm["w"][sl], model.nlc, model.npb, model.nep, model.lcids,
+                          model.pbids, model.epids, model.nsamples, model.exptimes, ldp, istar,
+                          model.weights, model.dk, model.klims[0], model.klims[1], model.dg, model.ze,
+                          nthreads=nthreads)
+
+
+def cpu_oracle_model(data):
+    import oracle
+    m = oracle.OracleRoadRunner('quadratic')
+    m.set_data(**data)
+    return m
+
+
+def run_cpu_baseline(data, prm, budget_s=12.0, npv_sample=512):
+    """The oracle's C port of rr_full on all host cores, on the first
+    npv_sample parameter vectors of the workload, repeated for ~budget_s."""
+    ncores = os.cpu_count() or 1
+    m = cpu_oracle_model(data)
+    cpu_rr_full(m, prm, 16, ncores)          # warm-up (thread pool, pages)
+    reps, t_total = 0, 0.0
+    while t_total < budget_s and reps < 50:
+        t = time.perf_counter()
+        cpu_rr_full(m, prm, npv_sample, ncores)
+        t_total += time.perf_counter() - t
+        reps += 1
+    npt = data["time"].size
+    value = reps * npv_sample * npt / t_total
+    return {"value": value, "unit": "model points/s", "cores": ncores, "kind": "port",
+            "sample": f"{npv_sample} of 8192 parameter vectors x {npt} times, {reps} repetitions, "
+                      f"{t_total:.1f} s (oracle/rr_oracle.c rr_full restatement, OpenMP, FP64)"}
+
+
+def impl_reference(args, rank):
+    if rank != 0:
+        return 0
+    data, prm = workload()
+    ncores = os.cpu_count() or 1
+    m = cpu_oracle_model(data)
+    npv_sample = 2048
+    npt = data["time"].size
+    for _ in range(args.warmup):
+        cpu_rr_full(m, prm, npv_sample, ncores)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_rr_full(m, prm, npv_sample, ncores)
+    dt = time.perf_counter() - t
+    value = args.steps * npv_sample * npt / dt
+    sample = (f"{npv_sample} of 8192 parameter vectors x {npt} times per step (oracle/rr_oracle.c "
+              f"rr_full restatement, OpenMP on {ncores} host threads, FP64)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "model points/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample_npv_per_step": npv_sample},
+            "cpu_baseline": {"value": value, "unit": "model points/s", "cores": ncores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "model points/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--npv", type=int, default=8192)
+    ap.add_argument("--npt", type=int, default=19700)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return impl_reference(args, rank)
+
+    import torch
+    import torch.distributed as dist
+    from pytransit_gb300 import RoadRunnerModel, _lib
+
+    torch.cuda.set_device(local_rank)
+    device = torch.device("cuda", local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=device)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # Each rank evaluates its own population (weak scaling, no collective on the data path).
+    data, prm = workload(args.npv, args.npt, seed=1234 + rank)
+    npv, npt = args.npv, args.npt
+    model = RoadRunnerModel('quadratic', precision='split', device=device)
+    model.set_data(**data)
+    dd = model._device_data(device)
+    tb = model._device_tables(device)
+    L = _lib.lib()
+    stream = torch.cuda.current_stream(device)
+    sp = _lib.stream_ptr(device)
+    nz, ng, nk = model.ze.size, model.ng, model.nk
+    nlc, npb, nep = model.nlc, model.npb, 1
+    dev = {n: torch.as_tensor(np.ascontiguousarray(v)).to(device) for n, v in prm.items()}
+    ldp32 = torch.empty((npv, npb, nz), dtype=torch.float32, device=device)
+    ist32 = torch.empty((npv, npb), dtype=torch.float32, device=device)
+    ldp64 = torch.empty((npv, npb, nz), dtype=torch.float64, device=device)
+    ist64 = torch.empty((npv, npb), dtype=torch.float64, device=device)
+    ldf = (npt + 3) // 4 * 4
+    flux32 = torch.empty((npv, ldf), dtype=torch.float32, device=device)
+    flux64 = torch.empty((npv, npt), dtype=torch.float64, device=device)
+    ws32 = torch.empty(L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng), dtype=torch.uint8, device=device)
+    ws64 = torch.empty(L.rr_full_f64_workspace_bytes(npv, npb, ng), dtype=torch.uint8, device=device)
+    P = _lib.ptr
+    kmin, kmax = float(model.klims[0]), float(model.klims[1])
+
+    def step_split(ev=None):
+        _lib.check(L.rr_ld_tables_f32(2, P(dev["ldc"]), npv, npb, 2, P(tb["mu"]), nz, P(ldp32), P(ist32), sp))
+        _lib.check(L.rr_prepare_split(dd["t_ref"], dd["t_absmax"], P(dev["k"]), 1, P(dev["t0"]), 1, nep,
+                                      P(dev["p"]), P(dev["a"]), P(dev["i"]), P(dev["e"]), P(dev["w"]), npv, nlc,
+                                      npb, P(dd["exptimes"]), P(ldp32), P(ist32), P(tb["W32"]), nk, ng, nz,
+                                      model.dk, kmin, kmax, P(tb["ze"]), P(ws32), ws32.numel(), sp))
+        if ev is not None:
+            ev[0].record(stream)
+        _lib.check(L.rr_flux_split(P(dd["times_ff"]), npt, P(dd["lcids"]), P(dd["pbids"]), P(dd["epids"]),
+                                   P(dd["nsamples"]), P(dd["exptimes"]), npv, nlc, npb, nep, ng, model.dg,
+                                   P(ws32), P(flux32), ldf, sp))
+        if ev is not None:
+            ev[1].record(stream)
+
+    def step_fp64():
+        _lib.check(L.rr_ld_tables_f64(2, P(dev["ldc"]), npv, npb, 2, P(tb["mu"]), nz, P(ldp64), P(ist64), sp))
+        _lib.check(L.rr_full_f64(P(dd["time"]), npt, P(dev["k"]), 1, P(dev["t0"]), 1, P(dev["p"]), P(dev["a"]),
+                                 P(dev["i"]), P(dev["e"]), P(dev["w"]), npv, nlc, npb, P(dd["lcids"]),
+                                 P(dd["pbids"]), P(dd["epids"]), P(dd["nsamples"]), P(dd["exptimes"]), P(ldp64),
+                                 P(ist64), P(tb["W64"]), nk, ng, nz, model.dk, kmin, kmax, model.dg, P(tb["ze"]),
+                                 P(ws64), ws64.numel(), P(flux64), npt, sp))
+
+    def timed(fn, steps, warmup, per_step_events=False):
+        for _ in range(warmup):
+            fn()
+        barrier()
+        torch.cuda.synchronize(device)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)] if per_step_events else None
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for s in range(steps):
+            if per_step_events:
+                fn(evs[s])
+            else:
+                fn()
+        t1.record(stream)
+        torch.cuda.synchronize(device)
+        barrier()
+        ms = t0.elapsed_time(t1)
+        kern = [a.elapsed_time(b) for a, b in evs] if per_step_events else None
+        return ms, kern
+
+    # --- split path, device-resident inputs (the headline `value`) ---
+    with ClockSampler(local_rank) as clk:
+        ms_split, kern_ms = timed(step_split, args.steps, args.warmup, per_step_events=True)
+    clocks = clk.summary()
+    ms_split = max_over_ranks(ms_split)
+    per_step_s = ms_split / 1e3 / args.steps
+    value = world * npv * npt / per_step_s
+
+    # --- plain FP64 path ---
+    fp64_steps = max(3, args.steps // 4)
+    ms64, _ = timed(step_fp64, fp64_steps, 2)
+    ms64 = max_over_ranks(ms64)
+    value64 = world * npv * npt / (ms64 / 1e3 / fp64_steps)
+
+    # accuracy of the split path on this workload, full size (max |dF| vs FP64)
+    step_split()
+    step_fp64()
+    torch.cuda.synchronize(device)
+    dF = float((flux32[:, :npt].double() - flux64).abs().max().item())
+    in_transit = float((flux64 < 1.0).double().mean().item())
+
+    # --- end to end through the public API: host params in, pinned host flux out ---
+    host_out = torch.empty((npv, npt), dtype=torch.float32, pin_memory=True)
+    e2e_prm = {n: np.ascontiguousarray(v) for n, v in prm.items()}
+
+    def step_e2e():
+        model.evaluate(e2e_prm["k"], e2e_prm["ldc"], e2e_prm["t0"], e2e_prm["p"], e2e_prm["a"],
+                       e2e_prm["i"], e2e_prm["e"], e2e_prm["w"], out=host_out)
+
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(args.warmup):
+        step_e2e()
+    barrier()
+    torch.cuda.synchronize(device)
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        step_e2e()
+    torch.cuda.synchronize(device)
+    e2e_s = max_over_ranks(time.perf_counter() - t) / e2e_steps
+    e2e_value = world * npv * npt / e2e_s
+    h2d = sum(v.size for v in prm.values()) * 8
+    d2h = npv * npt * 4
+
+    # --- roofline of the flux kernel ---
+    kern_avg_s = statistics.mean(kern_ms) / 1e3
+    s_out, s_tab = 4, 4
+    bytes_alg = (npv * npt * s_out + npt * (8 + 4) + npv * npb * (ng + 1) * s_tab
+                 + npv * (10 * 8 + nlc * 16))
+    achieved = bytes_alg / kern_avg_s / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profiled_traffic(npv, npt)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "model points/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 per-sample arithmetic, f64 orbit/phase data (split precision)",
+        "data": "synthetic (seeded; no public dataset)",
+        "config": {"workload": WORKLOAD, "npv_per_gpu": npv, "npt": npt, "npb": npb, "nlc": nlc,
+                   "nsamples": 1, "ld": "quadratic", "precision": "split",
+                   "l2": "no flush: each step writes npv*npt*4 B of flux (645 MB > 129 MB L2)",
+                   "parallelism": f"replicas x{world} (independent populations per GPU)"},
+        "fp64_path": {"value": value64, "unit": "model points/s", "ms_per_step": ms64 / fp64_steps},
+        "split_over_fp64": value / value64,
+        "max_abs_dF_vs_fp64": dF,
+        "in_transit_fraction": in_transit,
+        "e2e": {"value": e2e_value, "unit": "model points/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+                "path": "RoadRunnerModel.evaluate(numpy params, out=pinned host float32)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "flux_split_kernel", "kernel_ms": kern_avg_s * 1e3,
+                     "bytes_alg_per_launch": bytes_alg},
+        "clocks": clocks,
+        "gpu_launches": 4 * args.steps,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = run_cpu_baseline(data, prm)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

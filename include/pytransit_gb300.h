@@ -114,6 +114,31 @@ int rr_full_split(const float *times_ff, double t_ref, double t_absmax, int npt,
                   double kmin, double kmax, double dg, const double *z_edges, void *workspace,
                   size_t workspace_bytes, float *flux, int ldflux, void *stream);
 
+/* The two stages of rr_full_f64, callable separately (the workspace carries
+ * the per-parameter-vector tables from one to the other): the prologue of
+ * model_full.py:39-71 and the flux loop of model_full.py:75-99. */
+int rr_prepare_f64(const double *k, int nkc, const double *p, const double *a, const double *inc,
+                   const double *e, const double *w, int npv, int npb, const double *ldp,
+                   const double *weights, int nk, int ng, int nz, double dk, double kmin, double kmax,
+                   const double *z_edges, void *workspace, size_t workspace_bytes, void *stream);
+int rr_flux_f64(const double *times, int npt, const double *k, int nkc, const double *t0, int ldt0,
+                const double *p, int npv, int nlc, int npb, const int32_t *lcids, const int32_t *pbids,
+                const int32_t *epids, const int32_t *nsamples, const double *exptimes,
+                const double *istar, int ng, double dg, const void *workspace, double *flux, int ldflux,
+                void *stream);
+
+/* The two stages of rr_full_split. */
+int rr_prepare_split(double t_ref, double t_absmax, const double *k, int nkc, const double *t0, int ldt0,
+                     int nep, const double *p, const double *a, const double *inc, const double *e,
+                     const double *w, int npv, int nlc, int npb, const double *exptimes, const float *ldp,
+                     const float *istar, const float *weights, int nk, int ng, int nz, double dk,
+                     double kmin, double kmax, const double *z_edges, void *workspace,
+                     size_t workspace_bytes, void *stream);
+int rr_flux_split(const float *times_ff, int npt, const int32_t *lcids, const int32_t *pbids,
+                  const int32_t *epids, const int32_t *nsamples, const double *exptimes, int npv, int nlc,
+                  int npb, int nep, int ng, double dg, const void *workspace, float *flux, int ldflux,
+                  void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -490,6 +490,65 @@ static int check_common(int npt, int nkc, int npv, int nlc, int npb, int nk, int
   return RR_OK;
 }
 
+struct SplitTables {
+  float *orb, *box, *ep, *pb, *ldm;
+};
+
+static SplitTables carve_split(void* ws, int npv, int npb, int nlc, int nep, int ng) {
+  Carve cv(ws);
+  SplitTables t;
+  t.orb = cv.take<float>((size_t)npv * ORB32);
+  t.box = cv.take<float>((size_t)npv * nlc * 2);
+  t.ep = cv.take<float>((size_t)npv * nep * 2);
+  t.pb = cv.take<float>((size_t)npv * npb * 4);
+  t.ldm = cv.take<float>((size_t)npv * npb * ng);
+  return t;
+}
+
+int rr_prepare_f64(const double* k, int nkc, const double* p, const double* a, const double* inc,
+                   const double* e, const double* w, int npv, int npb, const double* ldp,
+                   const double* weights, int nk, int ng, int nz, double dk, double kmin, double kmax,
+                   const double* z_edges, void* workspace, size_t workspace_bytes, void* stream) {
+  if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
+  if (npv < 0 || npb < 1 || nk < 2 || ng < 2 || nz < 1 || nz > MAX_NZ || nkc < 1) return RR_ERR_ARG;
+  if (npv == 0) return RR_OK;
+  if (workspace_bytes < rr_full_f64_workspace_bytes(npv, npb, ng)) return RR_ERR_WORKSPACE;
+  cudaStream_t s = as_stream(stream);
+  Carve cv(workspace);
+  double* orb = cv.take<double>((size_t)npv * ORB64);
+  double* ldm = cv.take<double>((size_t)npv * npb * ng);
+  dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
+  ldm_kernel<double><<<lg, 128, 0, s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0,
+                                        nullptr, ldm);
+  OrbitArgs oa{};
+  oa.k = k; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w;
+  oa.nkc = nkc; oa.npv = npv; oa.npb = npb; oa.nz = nz;
+  oa.ldp = ldp; oa.ldp_is_f32 = 0; oa.orb64 = orb;
+  orbit_kernel<false><<<(npv + 31) / 32, 32, 0, s>>>(oa);
+  return check_launch("rr_prepare_f64");
+}
+
+int rr_flux_f64(const double* times, int npt, const double* k, int nkc, const double* t0, int ldt0,
+                const double* p, int npv, int nlc, int npb, const int32_t* lcids, const int32_t* pbids,
+                const int32_t* epids, const int32_t* nsamples, const double* exptimes,
+                const double* istar, int ng, double dg, const void* workspace, double* flux, int ldflux,
+                void* stream) {
+  if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
+  if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || nkc < 1 || ldflux < npt) return RR_ERR_ARG;
+  if (npv == 0 || npt == 0) return RR_OK;
+  Carve cv(const_cast<void*>(workspace));
+  double* orb = cv.take<double>((size_t)npv * ORB64);
+  double* ldm = cv.take<double>((size_t)npv * npb * ng);
+  FluxF64Args fa{};
+  fa.times = times; fa.k = k; fa.t0 = t0; fa.p = p; fa.exptimes = exptimes; fa.istar = istar;
+  fa.ldm = ldm; fa.orb64 = orb; fa.lcids = lcids; fa.pbids = pbids; fa.epids = epids;
+  fa.nsamples = nsamples; fa.npt = npt; fa.npv = npv; fa.nkc = nkc; fa.ldt0 = ldt0; fa.npb = npb;
+  fa.ng = ng; fa.ldflux = ldflux; fa.dg = dg; fa.flux = flux;
+  dim3 fg((npt + 255) / 256, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
+  flux_f64_kernel<<<fg, 256, 0, as_stream(stream)>>>(fa);
+  return check_launch("rr_flux_f64");
+}
+
 int rr_full_f64(const double* times, int npt, const double* k, int nkc, const double* t0, int ldt0,
                 const double* p, const double* a, const double* inc, const double* e, const double* w,
                 int npv, int nlc, int npb, const int32_t* lcids, const int32_t* pbids,
@@ -501,28 +560,56 @@ int rr_full_f64(const double* times, int npt, const double* k, int nkc, const do
   if (st) return st;
   if (npv == 0 || npt == 0) return RR_OK;
   if (workspace_bytes < rr_full_f64_workspace_bytes(npv, npb, ng)) return RR_ERR_WORKSPACE;
-  cudaStream_t s = as_stream(stream);
-  Carve cv(workspace);
-  double* orb = cv.take<double>((size_t)npv * ORB64);
-  double* ldm = cv.take<double>((size_t)npv * npb * ng);
+  st = rr_prepare_f64(k, nkc, p, a, inc, e, w, npv, npb, ldp, weights, nk, ng, nz, dk, kmin, kmax, z_edges,
+                      workspace, workspace_bytes, stream);
+  if (st) return st;
+  return rr_flux_f64(times, npt, k, nkc, t0, ldt0, p, npv, nlc, npb, lcids, pbids, epids, nsamples, exptimes,
+                     istar, ng, dg, workspace, flux, ldflux, stream);
+}
 
+int rr_prepare_split(double t_ref, double t_absmax, const double* k, int nkc, const double* t0, int ldt0,
+                     int nep, const double* p, const double* a, const double* inc, const double* e,
+                     const double* w, int npv, int nlc, int npb, const double* exptimes, const float* ldp,
+                     const float* istar, const float* weights, int nk, int ng, int nz, double dk,
+                     double kmin, double kmax, const double* z_edges, void* workspace,
+                     size_t workspace_bytes, void* stream) {
+  if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
+  if (npv < 0 || nlc < 1 || npb < 1 || nk < 2 || ng < 2 || nz < 1 || nz > MAX_NZ || nkc < 1 || nep < 1 ||
+      nep > ldt0)
+    return RR_ERR_ARG;
+  if (npv == 0) return RR_OK;
+  if (workspace_bytes < rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng)) return RR_ERR_WORKSPACE;
+  cudaStream_t s = as_stream(stream);
+  SplitTables t = carve_split(workspace, npv, npb, nlc, nep, ng);
   dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-  ldm_kernel<double><<<lg, 128, 0, s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0,
-                                        nullptr, ldm);
+  ldm_kernel<float><<<lg, 128, 0, s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0,
+                                       nullptr, t.ldm);
   OrbitArgs oa{};
   oa.k = k; oa.t0 = t0; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w; oa.exptimes = exptimes;
-  oa.nkc = nkc; oa.ldt0 = ldt0; oa.nep = 0; oa.npv = npv; oa.nlc = nlc; oa.npb = npb; oa.nz = nz;
-  oa.ldp = ldp; oa.ldp_is_f32 = 0; oa.orb64 = orb;
-  orbit_kernel<false><<<(npv + 31) / 32, 32, 0, s>>>(oa);
-  FluxF64Args fa{};
-  fa.times = times; fa.k = k; fa.t0 = t0; fa.p = p; fa.exptimes = exptimes; fa.istar = istar;
-  fa.ldm = ldm; fa.orb64 = orb; fa.lcids = lcids; fa.pbids = pbids; fa.epids = epids;
-  fa.nsamples = nsamples; fa.npt = npt; fa.nkc = nkc; fa.ldt0 = ldt0; fa.npb = npb; fa.ng = ng;
-  fa.ldflux = ldflux; fa.dg = dg; fa.flux = flux;
-  fa.npv = npv;
-  dim3 fg((npt + 255) / 256, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
-  flux_f64_kernel<<<fg, 256, 0, s>>>(fa);
-  return check_launch("rr_full_f64");
+  oa.nkc = nkc; oa.ldt0 = ldt0; oa.nep = nep; oa.npv = npv; oa.nlc = nlc; oa.npb = npb; oa.nz = nz;
+  oa.ldp = ldp; oa.ldp_is_f32 = 1; oa.orb32 = t.orb; oa.box32 = t.box; oa.ep32 = t.ep; oa.pb32 = t.pb;
+  oa.istar32 = istar; oa.t_ref = t_ref; oa.t_absmax = t_absmax;
+  orbit_kernel<true><<<(npv + 31) / 32, 32, 0, s>>>(oa);
+  return check_launch("rr_prepare_split");
+}
+
+int rr_flux_split(const float* times_ff, int npt, const int32_t* lcids, const int32_t* pbids,
+                  const int32_t* epids, const int32_t* nsamples, const double* exptimes, int npv, int nlc,
+                  int npb, int nep, int ng, double dg, const void* workspace, float* flux, int ldflux,
+                  void* stream) {
+  if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || nep < 1 || ldflux < npt) return RR_ERR_ARG;
+  if (npv == 0 || npt == 0) return RR_OK;
+  SplitTables t = carve_split(const_cast<void*>(workspace), npv, npb, nlc, nep, ng);
+  FluxSplitArgs fa{};
+  fa.times_ff = reinterpret_cast<const float2*>(times_ff);
+  fa.lcids = lcids; fa.pbids = pbids; fa.epids = epids; fa.nsamples = nsamples; fa.exptimes = exptimes;
+  fa.orb32 = t.orb; fa.box32 = t.box; fa.ep32 = t.ep; fa.pb32 = t.pb; fa.ldm = t.ldm;
+  fa.npt = npt; fa.npv = npv; fa.npb = npb; fa.nlc = nlc; fa.nep = nep; fa.ng = ng; fa.ldflux = ldflux;
+  fa.inv_dg = (float)(1.0 / dg); fa.flux = flux;
+  dim3 fg((npt + WARP_TILE * SPLIT_WARPS - 1) / (WARP_TILE * SPLIT_WARPS), npv < 65535 ? npv : 65535,
+          (npv + 65534) / 65535);
+  flux_split_kernel<<<fg, SPLIT_WARPS * 32, 0, as_stream(stream)>>>(fa);
+  return check_launch("rr_flux_split");
 }
 
 int rr_full_split(const float* times_ff, double t_ref, double t_absmax, int npt, const double* k, int nkc,
@@ -538,34 +625,12 @@ int rr_full_split(const float* times_ff, double t_ref, double t_absmax, int npt,
   if (nep < 1 || nep > ldt0) return RR_ERR_ARG;
   if (npv == 0 || npt == 0) return RR_OK;
   if (workspace_bytes < rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng)) return RR_ERR_WORKSPACE;
-  cudaStream_t s = as_stream(stream);
-  Carve cv(workspace);
-  float* orb = cv.take<float>((size_t)npv * ORB32);
-  float* box = cv.take<float>((size_t)npv * nlc * 2);
-  float* ep32 = cv.take<float>((size_t)npv * nep * 2);
-  float* pb32 = cv.take<float>((size_t)npv * npb * 4);
-  float* ldm = cv.take<float>((size_t)npv * npb * ng);
-
-  dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-  ldm_kernel<float><<<lg, 128, 0, s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0,
-                                       nullptr, ldm);
-  OrbitArgs oa{};
-  oa.k = k; oa.t0 = t0; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w; oa.exptimes = exptimes;
-  oa.nkc = nkc; oa.ldt0 = ldt0; oa.nep = nep; oa.npv = npv; oa.nlc = nlc; oa.npb = npb; oa.nz = nz;
-  oa.ldp = ldp; oa.ldp_is_f32 = 1; oa.orb32 = orb; oa.box32 = box; oa.ep32 = ep32; oa.pb32 = pb32;
-  oa.istar32 = istar; oa.t_ref = t_ref; oa.t_absmax = t_absmax;
-  orbit_kernel<true><<<(npv + 31) / 32, 32, 0, s>>>(oa);
-  FluxSplitArgs fa{};
-  fa.times_ff = reinterpret_cast<const float2*>(times_ff);
-  fa.lcids = lcids; fa.pbids = pbids; fa.epids = epids; fa.nsamples = nsamples; fa.exptimes = exptimes;
-  fa.orb32 = orb; fa.box32 = box; fa.ep32 = ep32; fa.pb32 = pb32; fa.ldm = ldm;
-  fa.npt = npt; fa.npb = npb; fa.nlc = nlc; fa.nep = nep; fa.ng = ng; fa.ldflux = ldflux;
-  fa.inv_dg = (float)(1.0 / dg); fa.flux = flux;
-  fa.npv = npv;
-  dim3 fg((npt + WARP_TILE * SPLIT_WARPS - 1) / (WARP_TILE * SPLIT_WARPS), npv < 65535 ? npv : 65535,
-          (npv + 65534) / 65535);
-  flux_split_kernel<<<fg, SPLIT_WARPS * 32, 0, s>>>(fa);
-  return check_launch("rr_full_split");
+  st = rr_prepare_split(t_ref, t_absmax, k, nkc, t0, ldt0, nep, p, a, inc, e, w, npv, nlc, npb, exptimes, ldp,
+                        istar, weights, nk, ng, nz, dk, kmin, kmax, z_edges, workspace, workspace_bytes,
+                        stream);
+  if (st) return st;
+  return rr_flux_split(times_ff, npt, lcids, pbids, epids, nsamples, exptimes, npv, nlc, npb, nep, ng, dg,
+                       workspace, flux, ldflux, stream);
 }
 
 }  // extern "C"

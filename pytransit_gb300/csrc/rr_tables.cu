@@ -85,7 +85,9 @@ __global__ void ld_tables_kernel(int law, const double* __restrict__ ldc, int np
     // 2*pi*trapezoid(z*I(mu(z)), z), mu = linspace(1, 0, 200), z = sqrt(1 - mu^2)
     R s = R(0), z0 = R(0), y0 = R(0);
     for (int i = 0; i < NTRAP; ++i) {
-      R m = (i == NTRAP - 1) ? R(0) : R(i) * (R(-1) / R(NTRAP - 1)) + R(1);
+      // (n-1-i)/(n-1): exactly 1 and 0 at the ends (a select of the end value
+      // was not honoured by the nvcc 13.0 -O3 build, leaving mu = -1.5e-17)
+      R m = R(NTRAP - 1 - i) / R(NTRAP - 1);
       R z = sqrt(R(1) - m * m);
       R y = z * ld_value<R>(law, m, pv, npar);
       if (i > 0) s += (z - z0) * (y + y0) / R(2);

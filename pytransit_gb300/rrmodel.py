@@ -232,16 +232,18 @@ class RoadRunnerModel(TransitModel):
                              f"with npv={npv}, npb={npb}; got {ldc.shape}.")
         return np.ascontiguousarray(ldc)
 
-    def _ld_tables(self, ldc, npv, npb, device, split):
-        """(ldp[npv, npb, nz], istar[npv, npb]) on the device (rrmodel.py:212-227)."""
+    def _ld_tables(self, ldc, npv, npb, device, split, ldc_d=None):
+        """(ldp[npv, npb, nz], istar[npv, npb]) on the device (rrmodel.py:212-227).
+        For a named law ``ldc_d`` is the [npv, npb, ncoef] array already on the device."""
         import torch
         from . import _lib
         tb = self._device_tables(device)
         nz = self.ze.size
         dt = torch.float32 if split else torch.float64
         if self.ld_law is not None:
-            ldc3 = self._shape_ldc(ldc, npv, npb)
-            ldc_d = torch.as_tensor(ldc3).to(device)
+            if ldc_d is None:
+                ldc_d = torch.as_tensor(self._shape_ldc(ldc, npv, npb)).to(device)
+            ldc3 = ldc_d
             ldp = torch.empty((npv, npb, nz), dtype=dt, device=device)
             istar = torch.empty((npv, npb), dtype=dt, device=device)
             fn = _lib.lib().rr_ld_tables_f32 if split else _lib.lib().rr_ld_tables_f64
@@ -273,33 +275,65 @@ class RoadRunnerModel(TransitModel):
         istar_d = torch.as_tensor(np.ascontiguousarray(istar)).to(device=device, dtype=dt)
         return ldp_d, istar_d
 
+    def _upload(self, arrays, device):
+        """Send the small per-call arrays in one host-to-device copy through a
+        reused pinned staging buffer; returns device views of the same shapes."""
+        import torch
+        names = [n for n, v in arrays.items() if v is not None]
+        sizes = [int(arrays[n].size) for n in names]
+        total = sum(sizes)
+        if getattr(self, '_pin', None) is None or self._pin.numel() < total or self._pin_dev.device != device:
+            n = max(total, 1024)
+            self._pin = torch.empty(n, dtype=torch.float64, pin_memory=True)
+            self._pin_dev = torch.empty(n, dtype=torch.float64, device=device)
+            self._pin_evt = None
+        if self._pin_evt is not None:
+            self._pin_evt.synchronize()      # the previous copy has left the staging buffer
+        hp = self._pin.numpy()
+        off = 0
+        for n, sz in zip(names, sizes):
+            hp[off:off + sz] = np.asarray(arrays[n], dtype=np.float64).reshape(-1)
+            off += sz
+        self._pin_dev[:total].copy_(self._pin[:total], non_blocking=True)
+        self._pin_evt = torch.cuda.Event()
+        self._pin_evt.record()
+        out, off = {}, 0
+        for n, sz in zip(names, sizes):
+            out[n] = self._pin_dev[off:off + sz].view(arrays[n].shape)
+            off += sz
+        return out
+
     # ------------------------------------------------------------------
     def evaluate(self, k: Union[float, ndarray], ldc: Union[ndarray, List], t0: Union[float, ndarray],
                  p: Union[float, ndarray], a: Union[float, ndarray], i: Union[float, ndarray],
-                 e: Union[float, ndarray] = 0.0, w: Union[float, ndarray] = 0.0, copy: bool = True):
+                 e: Union[float, ndarray] = 0.0, w: Union[float, ndarray] = 0.0, copy: bool = True,
+                 out=None):
         """Evaluate the transit model for one or many parameter vectors.
 
         Returns the modelled flux, [npt] for one parameter vector and
         [npv, npt] for many (squeezed as the reference does).  With copy=True a
         float64 numpy array; with copy=False the torch tensor on the GPU
-        (float64, or float32 in the split precision)."""
+        (float64, or float32 in the split precision).  ``out``: an optional
+        [npv, npt] torch tensor (pinned host memory or device) that receives the
+        flux; it is filled, synchronised and returned."""
         import torch
         from . import _lib
+        user_out = out
         device = self._cuda_device()
         k, t0, p, a, i, e, w = self._shape_params(k, t0, p, a, i, e, w)
         npv, npt, npb, nlc = p.size, self.npt, self.npb, self.nlc
         split = self.precision == 'split'
         tb = self._device_tables(device)
         dd = self._device_data(device)
-        ldp, istar = self._ld_tables(ldc, npv, npb, device, split)
-        args = {n: torch.as_tensor(v).to(device) for n, v in
-                dict(k=k, t0=t0, p=p, a=a, i=i, e=e, w=w).items()}
+        ldc3 = self._shape_ldc(ldc, npv, npb) if self.ld_law is not None else None
+        args = self._upload(dict(k=k, t0=t0, p=p, a=a, i=i, e=e, w=w, ldc=ldc3), device)
+        ldp, istar = self._ld_tables(ldc, npv, npb, device, split, args.get('ldc'))
         L = _lib.lib()
         stream = _lib.stream_ptr(device)
         nz = self.ze.size
         if split:
             ldf = (npt + 3) // 4 * 4
-            out = torch.empty((npv, ldf), dtype=torch.float32, device=device)
+            res = torch.empty((npv, ldf), dtype=torch.float32, device=device)
             nep = t0.shape[1]
             wsb = L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, self.ng)
             ws = self._workspace(wsb, device)
@@ -311,10 +345,10 @@ class RoadRunnerModel(TransitModel):
                                  _lib.ptr(dd['nsamples']), _lib.ptr(dd['exptimes']), _lib.ptr(ldp),
                                  _lib.ptr(istar), _lib.ptr(tb['W32']), self.nk, self.ng, nz, self.dk,
                                  float(self.klims[0]), float(self.klims[1]), self.dg, _lib.ptr(tb['ze']),
-                                 _lib.ptr(ws), ws.numel(), _lib.ptr(out), ldf, stream)
-            out = out[:, :npt]
+                                 _lib.ptr(ws), ws.numel(), _lib.ptr(res), ldf, stream)
+            res = res[:, :npt]
         else:
-            out = torch.empty((npv, npt), dtype=torch.float64, device=device)
+            res = torch.empty((npv, npt), dtype=torch.float64, device=device)
             wsb = L.rr_full_f64_workspace_bytes(npv, npb, self.ng)
             ws = self._workspace(wsb, device)
             st = L.rr_full_f64(_lib.ptr(dd['time']), npt, _lib.ptr(args['k']), k.shape[1],
@@ -324,9 +358,14 @@ class RoadRunnerModel(TransitModel):
                                _lib.ptr(dd['nsamples']), _lib.ptr(dd['exptimes']), _lib.ptr(ldp),
                                _lib.ptr(istar), _lib.ptr(tb['W64']), self.nk, self.ng, nz, self.dk,
                                float(self.klims[0]), float(self.klims[1]), self.dg, _lib.ptr(tb['ze']),
-                               _lib.ptr(ws), ws.numel(), _lib.ptr(out), npt, stream)
+                               _lib.ptr(ws), ws.numel(), _lib.ptr(res), npt, stream)
         _lib.check(st, "rr_full")
-        out = out.squeeze()
+        if user_out is not None:
+            src = res if user_out.dtype == res.dtype else res.to(user_out.dtype)
+            user_out.view(npv, npt).copy_(src, non_blocking=True)
+            torch.cuda.current_stream(device).synchronize()
+            return user_out
+        res = res.squeeze()
         if copy:
-            return out.to(torch.float64).cpu().numpy()
-        return out
+            return res.to(torch.float64).cpu().numpy()
+        return res
