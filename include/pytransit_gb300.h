@@ -139,6 +139,37 @@ int rr_flux_split(const float *times_ff, int npt, const int32_t *lcids, const in
                   int npb, int nep, int ng, double dg, const void *workspace, float *flux, int ldflux,
                   void *stream);
 
+/* ---- no-allocation variant ------------------------------------------------- */
+
+/* No counterpart in the reference: an addition for callers that cannot
+ * allocate GPU memory themselves (a plugin host that owns the device and
+ * passes a plugin only its inputs and outputs, a pool-based runtime that
+ * forbids raw cudaMalloc, or a latency-bound loop where cudaMalloc's possible
+ * device synchronisation is not acceptable).
+ *
+ * Same model and arguments as rr_full_split, without the workspace: the
+ * per-parameter-vector tables live in a fixed file-scope device array of
+ * rr_full_split_noalloc_max_bytes() bytes (32 MiB) that every GPU loading the
+ * library holds until process exit.  The caller still passes inputs and
+ * outputs.  Returns RR_ERR_WORKSPACE, before launching anything, when
+ * rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng) exceeds that size.
+ * It calls no cudaMalloc/cudaFree.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the one
+ * array, which keeps the last call's contents (nothing in it needs clearing:
+ * every table is written before it is read); calls that overlap on the GPU,
+ * on different streams or host threads, race on it. */
+size_t rr_full_split_noalloc_max_bytes(void);
+int rr_full_split_noalloc(const float *times_ff, double t_ref, double t_absmax, int npt,
+                          const double *k, int nkc, const double *t0, int ldt0, int nep,
+                          const double *p, const double *a, const double *inc, const double *e,
+                          const double *w, int npv, int nlc, int npb, const int32_t *lcids,
+                          const int32_t *pbids, const int32_t *epids, const int32_t *nsamples,
+                          const double *exptimes, const float *ldp, const float *istar,
+                          const float *weights, int nk, int ng, int nz, double dk, double kmin,
+                          double kmax, double dg, const double *z_edges, float *flux, int ldflux,
+                          void *stream);
+
 #ifdef __cplusplus
 }
 #endif
