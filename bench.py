@@ -153,14 +153,14 @@ def cpu_oracle_model(data):
     return m
 
 
-def run_cpu_baseline(data, prm, budget_s=12.0, npv_sample=512):
+def run_cpu_baseline(data, prm, budget_s=12.0, npv_sample=8192):
     """The oracle's C port of rr_full on all host cores, on the first
     npv_sample parameter vectors of the workload, repeated for ~budget_s."""
     ncores = os.cpu_count() or 1
     m = cpu_oracle_model(data)
     cpu_rr_full(m, prm, 16, ncores)          # warm-up (thread pool, pages)
     reps, t_total = 0, 0.0
-    while t_total < budget_s and reps < 50:
+    while t_total < budget_s and reps < 1000:
         t = time.perf_counter()
         cpu_rr_full(m, prm, npv_sample, ncores)
         t_total += time.perf_counter() - t
@@ -270,12 +270,12 @@ def main():
         _lib.check(L.rr_ld_tables_f32(2, P(dev["ldc"]), npv, npb, 2, P(tb["mu"]), nz, P(ldp32), P(ist32), sp))
         _lib.check(L.rr_prepare_split(dd["t_ref"], dd["t_absmax"], P(dev["k"]), 1, P(dev["t0"]), 1, nep,
                                       P(dev["p"]), P(dev["a"]), P(dev["i"]), P(dev["e"]), P(dev["w"]), npv, nlc,
-                                      npb, P(dd["exptimes"]), P(ldp32), P(ist32), P(tb["W32"]), nk, ng, nz,
-                                      model.dk, kmin, kmax, P(tb["ze"]), P(ws32), ws32.numel(), sp))
+                                      npb, P(dd["pbids"]), P(dd["epids"]), P(dd["nsamples"]), P(dd["exptimes"]),
+                                      P(ldp32), P(ist32), P(tb["W32"]), nk, ng, nz, model.dk, kmin, kmax,
+                                      P(tb["ze"]), P(ws32), ws32.numel(), sp))
         if ev is not None:
             ev[0].record(stream)
-        _lib.check(L.rr_flux_split(P(dd["times_ff"]), npt, P(dd["lcids"]), P(dd["pbids"]), P(dd["epids"]),
-                                   P(dd["nsamples"]), P(dd["exptimes"]), npv, nlc, npb, nep, ng, model.dg,
+        _lib.check(L.rr_flux_split(P(dd["times_ff"]), npt, P(dd["lcids"]), npv, nlc, npb, ng, model.dg,
                                    P(ws32), P(flux32), ldf, sp))
         if ev is not None:
             ev[1].record(stream)

@@ -65,9 +65,15 @@ int rr_weights_3d(int nk, double kmin, double kmax, const double *ze, int nz, in
 /* ---- data (set_data) ----------------------------------------------------- */
 
 /* Part of TransitModel.set_data (pytransit/models/transitmodel.py:56-125) for
- * the split-precision path: times_ff[2*i] = hi, [2*i+1] = lo with
- * hi + lo = times[i] - t_ref to ~2^-48 relative (FP32 pair). */
-int rr_time_split(const double *times, int npt, double t_ref, float *times_ff, void *stream);
+ * the split-precision path.  times_ff holds rr_time_split_floats(npt) floats:
+ * first the FP32 pairs times_ff[2*i] = hi, [2*i+1] = lo with
+ * hi + lo = times[i] - t_ref to ~2^-48 relative, then (at float offset
+ * 2 * round_up(npt, 2)) one float4 per 128-point tile: the tile's smallest and
+ * largest hi and its light-curve id (int bits), or -1 when the tile spans
+ * several light curves. */
+size_t rr_time_split_floats(int npt);
+int rr_time_split(const double *times, const int32_t *lcids, int npt, double t_ref, float *times_ff,
+                  void *stream);
 
 /* ---- limb-darkening layer -------------------------------------------------- */
 
@@ -127,17 +133,53 @@ int rr_flux_f64(const double *times, int npt, const double *k, int nkc, const do
                 const double *istar, int ng, double dg, const void *workspace, double *flux, int ldflux,
                 void *stream);
 
-/* The two stages of rr_full_split. */
+/* The two stages of rr_full_split: the prologue writes the per-parameter-vector
+ * and per-(pv, light curve) tables into the workspace, the flux stage reads
+ * only those tables, the FP32-pair times and the light-curve ids. */
 int rr_prepare_split(double t_ref, double t_absmax, const double *k, int nkc, const double *t0, int ldt0,
                      int nep, const double *p, const double *a, const double *inc, const double *e,
-                     const double *w, int npv, int nlc, int npb, const double *exptimes, const float *ldp,
-                     const float *istar, const float *weights, int nk, int ng, int nz, double dk,
-                     double kmin, double kmax, const double *z_edges, void *workspace,
+                     const double *w, int npv, int nlc, int npb, const int32_t *pbids,
+                     const int32_t *epids, const int32_t *nsamples, const double *exptimes,
+                     const float *ldp, const float *istar, const float *weights, int nk, int ng, int nz,
+                     double dk, double kmin, double kmax, const double *z_edges, void *workspace,
                      size_t workspace_bytes, void *stream);
-int rr_flux_split(const float *times_ff, int npt, const int32_t *lcids, const int32_t *pbids,
-                  const int32_t *epids, const int32_t *nsamples, const double *exptimes, int npv, int nlc,
-                  int npb, int nep, int ng, double dg, const void *workspace, float *flux, int ldflux,
-                  void *stream);
+int rr_flux_split(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb, int ng,
+                  double dg, const void *workspace, float *flux, int ldflux, void *stream);
+
+/* ---- Gaussian log-likelihood and its gradient ----------------------------- */
+
+/* Fused model + Gaussian log-likelihood per parameter vector
+ * (pytransit/lpf/loglikelihood/wnloglikelihood.py:23-35, lpf.py:51-66):
+ *   lnl[pv] = sum_i -log(sigma_lc(i)) - log(2 pi)/2 - ((obs_i - flux[pv, i]) / sigma_lc(i))^2 / 2
+ * with sigma[nlc] one noise level per light curve; the flux is never stored.
+ * With grad != NULL also d lnl / d theta, grad[npv, ngrad] with columns
+ * [k (nkc)][t0 (nep)][p, a, i, e, w][ldc (npb x npar)], ngrad =
+ * rr_lnlike_ngrad(); the gradient is that of the discretised model (table
+ * interpolations, kite area, orbit Taylor coefficients), recomputing z per
+ * sample.  The reference has no adjoint (its dfdk/dfdb, common.py:105-128, are
+ * unused partials).  Named LD laws only (law, ldc[npv, npb, npar], npar <= 4);
+ * ldp/istar as from rr_ld_tables_*. */
+int rr_lnlike_ngrad(int nkc, int nep, int npb, int npar);
+size_t rr_lnlike_workspace_bytes(int split, int npv, int npb, int nlc, int nep, int ng, int npar, int npt,
+                                 int nkc);
+int rr_lnlike_f64(int law, const double *ldc, int npar, const double *mu, const double *times, int npt,
+                  const double *k, int nkc, const double *t0, int ldt0, int nep, const double *p,
+                  const double *a, const double *inc, const double *e, const double *w, int npv, int nlc,
+                  int npb, const int32_t *lcids, const int32_t *pbids, const int32_t *epids,
+                  const int32_t *nsamples, const double *exptimes, const double *ldp, const double *istar,
+                  const double *weights, int nk, int ng, int nz, double dk, double kmin, double kmax,
+                  double dg, const double *z_edges, const double *obs, const double *sigma, void *workspace,
+                  size_t workspace_bytes, double *lnl, double *grad, void *stream);
+/* Same, split precision (FP32 per-sample arithmetic and residuals formed from
+ * the deficit, FP64 block sums). */
+int rr_lnlike_split(int law, const double *ldc, int npar, const double *mu, const float *times_ff,
+                    double t_ref, double t_absmax, int npt, const double *k, int nkc, const double *t0,
+                    int ldt0, int nep, const double *p, const double *a, const double *inc, const double *e,
+                    const double *w, int npv, int nlc, int npb, const int32_t *lcids, const int32_t *pbids,
+                    const int32_t *epids, const int32_t *nsamples, const double *exptimes, const float *ldp,
+                    const float *istar, const float *weights, int nk, int ng, int nz, double dk, double kmin,
+                    double kmax, double dg, const double *z_edges, const double *obs, const double *sigma,
+                    void *workspace, size_t workspace_bytes, double *lnl, double *grad, void *stream);
 
 /* ---- no-allocation variant ------------------------------------------------- */
 

@@ -28,7 +28,9 @@ def _sig(L):
     L.rr_status_string.restype = C.c_char_p
     L.rr_last_cuda_error.restype = C.c_char_p
     L.rr_weights_3d.argtypes = [_i, _d, _d, _vp, _i, _i, _vp, _vp, C.POINTER(_d), C.POINTER(_d), _vp]
-    L.rr_time_split.argtypes = [_vp, _i, _d, _vp, _vp]
+    L.rr_time_split_floats.argtypes = [_i]
+    L.rr_time_split_floats.restype = _sz
+    L.rr_time_split.argtypes = [_vp, _vp, _i, _d, _vp, _vp]
     for n in ("rr_ld_tables_f64", "rr_ld_tables_f32"):
         getattr(L, n).argtypes = [_i, _vp, _i, _i, _i, _vp, _i, _vp, _vp, _vp]
     L.rr_full_f64_workspace_bytes.argtypes = [_i, _i, _i]
@@ -46,9 +48,8 @@ def _sig(L):
     L.rr_flux_f64.argtypes = ([_vp, _i, _vp, _i, _vp, _i, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i,
                                _d, _vp, _vp, _i, _vp])
     L.rr_prepare_split.argtypes = ([_d, _d, _vp, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp,
-                                    _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _vp, _vp, _sz, _vp])
-    L.rr_flux_split.argtypes = ([_vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp, _i,
-                                 _vp])
+                                    _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _vp, _vp, _sz, _vp])
+    L.rr_flux_split.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _vp, _i, _vp]
     for name, args in _EXTRA_SIGNATURES.items():
         if hasattr(L, name):
             getattr(L, name).argtypes = args[0]

@@ -63,6 +63,30 @@ __device__ inline R ccia_star(R k, R z, R& kappa0) {
   return R(CUDART_NAN);
 }
 
+// The same area with its partial derivatives: dA/dk = 2 k kappa0 (the
+// reference's dfdk, common.py:105-114) and dA/dz = -2 A_kite / z (its dfdb,
+// common.py:117-128).
+template <typename R>
+__device__ inline R ccia_star_grad(R k, R z, R& dadk, R& dadz) {
+  const R one = R(1);
+  const R pi = R(PI);
+  if (one + k <= z) { dadk = R(0); dadz = R(0); return R(0); }
+  if (fabs(one - k) < z && z <= one + k) {
+    R x, y, w;
+    tsort<R>(one, k, z, x, y, w);
+    R a_kite = R(0.5) * sqrt((x + (y + w)) * (w - (x - y)) * (w + (x - y)) * (x + (y - w)));
+    R k0 = atan2(R(2) * a_kite, (k - one) * (k + one) + z * z);
+    R k1 = atan2(R(2) * a_kite, (one - k) * (one + k) + z * z);
+    dadk = R(2) * k * k0;
+    dadz = -R(2) * a_kite / z;
+    return one * one * k1 + k * k * k0 - a_kite;
+  }
+  if (z <= one - k) { dadk = R(2) * pi * k; dadz = R(0); return pi * k * k; }
+  if (z <= k - one) { dadk = R(0); dadz = R(0); return pi; }
+  dadk = dadz = R(CUDART_NAN);
+  return R(CUDART_NAN);
+}
+
 // interpolate_mean_limb_darkening_s, common.py:225-233.  The reference reads
 // lda[ng] for g in [1-1e-7, 1]; the index is clamped to ng-2 here.
 __device__ inline double interp_ldm_f64(double g, double dg, const double* lda, int ng) {
@@ -140,6 +164,72 @@ __device__ inline bool ld_integral(int law, const R* pv, R& istar) {
   return false;
 }
 
+// Derivative of the LD profile I(mu) with respect to coefficient j (for the
+// adjoint).  Derived from the laws of ldmodels.py:23-140.
+template <typename R>
+__device__ inline R ld_dvalue(int law, R mu, const R* pv, int npar, int j) {
+  const R one = R(1);
+  switch (law) {
+    case LD_LINEAR: return -(one - mu);
+    case LD_QUADRATIC: return j == 0 ? -(one - mu) : -(one - mu) * (one - mu);
+    case LD_QUADRATIC_TRI: {
+      R a = sqrt(pv[0]), b = R(2) * pv[1];
+      if (j == 0) return -(b / (R(2) * a)) * (one - mu) - ((one - b) / (R(2) * a)) * (one - mu) * (one - mu);
+      return -R(2) * a * (one - mu) + R(2) * a * (one - mu) * (one - mu);
+    }
+    case LD_NONLINEAR:
+      switch (j) {
+        case 0: return -(one - sqrt(mu));
+        case 1: return -(one - mu);
+        case 2: return -(one - pow(mu, R(1.5)));
+        default: return -(one - mu * mu);
+      }
+    case LD_GENERAL: return one - pow(mu, R(j + 1));
+    case LD_SQUARE_ROOT: return j == 0 ? -(one - mu) : -(one - sqrt(mu));
+    case LD_LOGARITHMIC: return j == 0 ? -(one - mu) : -mu * log(mu);
+    case LD_EXPONENTIAL: return j == 0 ? -(one - mu) : -one / (one - exp(mu));
+    case LD_POWER_2: {
+      R ma = pow(mu, pv[1]);
+      return j == 0 ? -(one - ma) : pv[0] * ma * log(mu);
+    }
+    case LD_POWER_2_PM: {
+      R c = one - pv[0] + pv[1];
+      R a = log2(c / pv[1]);
+      R ma = pow(mu, a);
+      R dIdc = -(one - ma), dIda = c * ma * log(mu);
+      const R il2 = R(1.4426950408889634);  // 1 / ln 2
+      if (j == 0) return -dIdc + dIda * (-il2 / c);
+      return dIdc + dIda * il2 * (one / c - one / pv[1]);
+    }
+  }
+  return R(0);
+}
+
+// Derivative of the analytic disk integral with respect to coefficient j;
+// false for laws integrated numerically.
+template <typename R>
+__device__ inline bool ld_dintegral(int law, const R* pv, int j, R& d) {
+  const R twopi = R(2.0 * PI);
+  switch (law) {
+    case LD_UNIFORM: d = R(0); return true;
+    case LD_LINEAR: d = twopi / R(6) * R(-2); return true;
+    case LD_QUADRATIC: d = j == 0 ? twopi / R(12) * R(-2) : -twopi / R(12); return true;
+    case LD_QUADRATIC_TRI: {
+      R a = sqrt(pv[0]), b = R(2) * pv[1];
+      if (j == 0) d = twopi / R(12) * (R(-2) * (b / (R(2) * a)) - (R(1) - b) / (R(2) * a));
+      else d = twopi / R(12) * (R(-2) * a);
+      return true;
+    }
+    case LD_POWER_2: {
+      R N = -pv[0] * pv[1] + pv[1] + R(2), D = R(2) * pv[1] + R(4);
+      if (j == 0) d = twopi * (-pv[1]) / D;
+      else d = twopi * ((R(1) - pv[0]) * D - R(2) * N) / (D * D);
+      return true;
+    }
+  }
+  return false;
+}
+
 // ---------------------------------------------------------------------------
 // Orbit layer: Taylor coefficients of the sky position about conjunction
 // ---------------------------------------------------------------------------
@@ -209,6 +299,11 @@ __device__ inline double contact_point(double k, int point, const double* c) {
   return t1;
 }
 
+// The same bisection on the FP32 coefficients, for the split path: the contact
+// times only place the bounding box, which is padded by 0.003 d beyond
+// contact, so a ~1e-7 d error in them changes no flux value.
+__device__ inline float contact_point_f32(float k, int point, const float* c);
+
 // ---------------------------------------------------------------------------
 // Float-float helpers (error-free transformations, Knuth / Dekker)
 // ---------------------------------------------------------------------------
@@ -229,6 +324,29 @@ __device__ __forceinline__ float sep_c_f32(float t, const float* c) {
   float x = fmaf(t, fmaf(t, fmaf(t, fmaf(t, c[4], c[3]), c[2]), c[1]), c[0]);
   float y = fmaf(t, fmaf(t, fmaf(t, fmaf(t, c[9], c[8]), c[7]), c[6]), c[5]);
   return sqrtf(fmaf(x, x, y * y));
+}
+
+__device__ inline float contact_point_f32(float k, int point, const float* c) {
+  const float s = (point == 1 || point == 2) ? -1.0f : 1.0f;
+  const float zt = (point == 1 || point == 4) ? 1.0f + k : 1.0f - k;
+  float t0 = 0.0f;
+  float t2 = s * 2.0f / c[1];
+  float t1 = 0.5f * t2;
+  float z0 = sep_c_f32(t0, c) - zt;
+  float z1 = sep_c_f32(t1, c) - zt;
+  for (int i = 0; fabsf(t2 - t0) > 1e-6f && i < 100; ++i) {
+    if (z0 * z1 < 0.0f) {
+      t2 = t1;
+      t1 = 0.5f * (t0 + t1);
+      z1 = sep_c_f32(t1, c) - zt;
+    } else {
+      t0 = t1;
+      t1 = 0.5f * (t1 + t2);
+      z0 = z1;
+      z1 = sep_c_f32(t1, c) - zt;
+    }
+  }
+  return t1;
 }
 
 }  // namespace rr

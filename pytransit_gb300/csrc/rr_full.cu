@@ -19,7 +19,10 @@ constexpr int MAX_NZ = 64;      // radial grid points staged in shared memory
 // common.py:153-185) when k is outside [kmin, kmax] (mode 0) or when ik+1
 // would run past the table.  mode 1: the transmission-spectroscopy rule
 // kmin <= k <= kmax_pv[pv] (model_trspec.py:48); mode 2: always the 2D table.
-// Grid (npv, ceil(npb / LDM_PBB)), 128 threads.
+// One block per (pv, group of LDM_PBB passbands): the k-interpolated weight
+// slab is staged in shared memory with coalesced loads (rows padded to nz+1
+// words so the dot products are free of bank conflicts), then every (pb, g)
+// output is a dot product from shared memory.
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(128)
@@ -27,15 +30,15 @@ ldm_kernel(const R* __restrict__ ldp, int npb, int nz, const double* __restrict_
            const R* __restrict__ W, int nk, int ng, double dk, double kmin, double kmax,
            const double* __restrict__ ze, int mode, const double* __restrict__ kmax_pv,
            R* __restrict__ ldm) {
-  __shared__ R l[LDM_PBB][MAX_NZ];
-  __shared__ double zes[MAX_NZ];
+  extern __shared__ __align__(16) unsigned char ldm_smem[];
+  R* Wk = reinterpret_cast<R*>(ldm_smem);                  // [ng][nz + 1]
+  R* l = Wk + (size_t)ng * (nz + 1);                       // [LDM_PBB][nz]
+  const int ldw = nz + 1;
   const int pv = blockIdx.x;
   const int pb0 = blockIdx.y * LDM_PBB;
   const int nb = min(LDM_PBB, npb - pb0);
   for (int i = threadIdx.x; i < nb * nz; i += blockDim.x)
-    l[i / nz][i % nz] = ldp[((size_t)pv * npb + pb0 + i / nz) * nz + i % nz];
-  for (int i = threadIdx.x; i < nz; i += blockDim.x) zes[i] = ze[i];
-  __syncthreads();
+    l[i] = ldp[((size_t)pv * npb + pb0) * nz + i];
 
   const double k = kw[(size_t)pv * kw_stride];
   int ik = -1;
@@ -46,41 +49,49 @@ ldm_kernel(const R* __restrict__ ldp, int npb, int nz, const double* __restrict_
     ak = (k - kmin - ik * dk) / dk;
     if (ik + 1 >= nk || ik < 0) ik = -1;
   }
-  R* out = ldm + ((size_t)pv * npb + pb0) * ng;
   if (ik >= 0) {
     const R* W0 = W + (size_t)ik * ng * nz;
     const R* W1 = W0 + (size_t)ng * nz;
-    for (int j = threadIdx.x; j < nb * ng; j += blockDim.x) {
-      int b = j / ng, g = j % ng;
-      R d0 = R(0), d1 = R(0);
-      const R* w0 = W0 + (size_t)g * nz;
-      const R* w1 = W1 + (size_t)g * nz;
-      for (int z = 0; z < nz; ++z) {
-        d0 += __ldg(w0 + z) * l[b][z];
-        d1 += __ldg(w1 + z) * l[b][z];
-      }
-      out[(size_t)b * ng + g] = (R(1) - (R)ak) * d0 + (R)ak * d1;
-    }
+    const R a1 = (R)ak, a0 = R(1) - (R)ak;
+    for (int i = threadIdx.x; i < ng * nz; i += blockDim.x)
+      Wk[(i / nz) * ldw + (i % nz)] = a0 * __ldg(W0 + i) + a1 * __ldg(W1 + i);
   } else {
-    // 2D table at this k, row by row in FP64: w_i = (A(ze_i) - A(ze_{i-1})) / sum
+    // 2D table at this k, one row per thread in FP64: w_i = (A(ze_i) - A(ze_{i-1})) / sum
     const double gstep = (1.0 - 1e-7) / (double)(ng - 1);
     for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-      double gg = (g == ng - 1) ? (1.0 - 1e-7) : (double)g * gstep;
+      double gg = (double)g * gstep;
+      if (g == ng - 1) gg = 1.0 - 1e-7;
       double bb = gg * (1.0 + k);
-      double acc[LDM_PBB] = {0.0, 0.0, 0.0, 0.0};
-      double a0 = cci_acos(zes[0], k, bb);
+      double a0 = cci_acos(ze[0], k, bb);
       double s = a0;
-      for (int b = 0; b < nb; ++b) acc[b] = a0 * (double)l[b][0];
+      R* row = Wk + (size_t)g * ldw;
+      row[0] = (R)a0;
       for (int z = 1; z < nz; ++z) {
-        double a1 = cci_acos(zes[z], k, bb);
+        double a1 = cci_acos(ze[z], k, bb);
         double wz = a1 - a0;
         a0 = a1;
         s += wz;
-        for (int b = 0; b < nb; ++b) acc[b] += wz * (double)l[b][z];
+        row[z] = (R)wz;
       }
-      for (int b = 0; b < nb; ++b) out[(size_t)b * ng + g] = (R)(acc[b] / s);
+      // normalise in FP64 from the stored differences (exact for R = double)
+      for (int z = 0; z < nz; ++z) row[z] = (R)((double)row[z] / s);
     }
   }
+  __syncthreads();
+  R* out = ldm + ((size_t)pv * npb + pb0) * ng;
+  for (int j = threadIdx.x; j < nb * ng; j += blockDim.x) {
+    const int b = j / ng, g = j % ng;
+    const R* row = Wk + (size_t)g * ldw;
+    const R* lb = l + b * nz;
+    R d = R(0);
+    for (int z = 0; z < nz; ++z) d += row[z] * lb[z];
+    out[(size_t)b * ng + g] = d;
+  }
+}
+
+template <typename R>
+static size_t ldm_smem_bytes(int ng, int nz) {
+  return sizeof(R) * ((size_t)ng * (nz + 1) + (size_t)LDM_PBB * nz);
 }
 
 // ---------------------------------------------------------------------------
@@ -89,13 +100,14 @@ ldm_kernel(const R* __restrict__ ldp, int npb, int nz, const double* __restrict_
 // ---------------------------------------------------------------------------
 struct OrbitArgs {
   const double *k, *t0, *p, *a, *inc, *e, *w, *exptimes;
+  const int32_t *pbids, *epids, *nsamples;
   int nkc, ldt0, nep, npv, nlc, npb, nz;
   const void* ldp;       // validity probe ldp[pv, 0, 0] (double or float)
   int ldp_is_f32;
   // plain FP64 path
   double* orb64;
   // split path
-  float *orb32, *box32, *ep32, *pb32;
+  float *orb32, *lc32;
   const float* istar32;
   double t_ref, t_absmax;
 };
@@ -109,14 +121,21 @@ __global__ void orbit_kernel(OrbitArgs A) {
                             : isnan(((const double*)A.ldp)[(size_t)pv * A.npb * A.nz]);
   bool valid = !(isnan(a) || a <= 1.0 || e < 0.0 || ldbad);
   double c[10];
+  float cf[10];
   double t1 = 0.0, t4 = 0.0;
   double k0 = A.k[(size_t)pv * A.nkc];
   if (valid) {
     solve2d_conj(p, a, A.inc[pv], e, A.w[pv], c);
-    t1 = contact_point(k0, 1, c);
-    t4 = contact_point(k0, 4, c);
+    for (int i = 0; i < 10; ++i) cf[i] = (float)c[i];
+    if (SPLIT) {
+      t1 = contact_point_f32((float)k0, 1, cf);
+      t4 = contact_point_f32((float)k0, 4, cf);
+    } else {
+      t1 = contact_point(k0, 1, c);
+      t4 = contact_point(k0, 4, c);
+    }
   } else {
-    for (int i = 0; i < 10; ++i) c[i] = 0.0;
+    for (int i = 0; i < 10; ++i) { c[i] = 0.0; cf[i] = 0.0f; }
   }
   if (!SPLIT) {
     double* o = A.orb64 + (size_t)pv * ORB64;
@@ -127,44 +146,48 @@ __global__ void orbit_kernel(OrbitArgs A) {
     return;
   }
   float* o = A.orb32 + (size_t)pv * ORB32;
-  for (int i = 0; i < 10; ++i) o[i] = (float)c[i];
+  for (int i = 0; i < 10; ++i) o[i] = cf[i];
   float p_hi = __double2float_rn(p);
   float p_lo = __double2float_rn(p - (double)p_hi);
   o[10] = p_hi;
   o[11] = p_lo;
   o[12] = __double2float_rn(1.0 / p);
-  // epochs: d0 = t0 - t_ref as an FP32 pair
   double d0max = 0.0;
-  for (int ep = 0; ep < A.nep; ++ep) {
-    double d0 = A.t0[(size_t)pv * A.ldt0 + ep] - A.t_ref;
-    float hi = __double2float_rn(d0);
-    A.ep32[((size_t)pv * A.nep + ep) * 2 + 0] = hi;
-    A.ep32[((size_t)pv * A.nep + ep) * 2 + 1] = __double2float_rn(d0 - (double)hi);
-    d0max = fmax(d0max, fabs(d0));
-  }
+  for (int ep = 0; ep < A.nep; ++ep) d0max = fmax(d0max, fabs(A.t0[(size_t)pv * A.ldt0 + ep] - A.t_ref));
   // Bound of |fast-test tc - true tc|: 2^-24 (4 (T + |d0|) + 2 p), doubled.
-  double err = ldexp(1.0, -21) * (A.t_absmax + d0max + p) + 1e-9;
+  const double err = ldexp(1.0, -21) * (A.t_absmax + d0max + p) + 1e-9;
   o[13] = (float)err;
   int flags = valid ? FLAG_VALID : 0;
   for (int lc = 0; lc < A.nlc; ++lc) {
-    double pad = 0.003 + A.exptimes[lc];
-    double lo = t1 - pad, hi = t4 + pad;
-    A.box32[((size_t)pv * A.nlc + lc) * 2 + 0] = (float)lo;
-    A.box32[((size_t)pv * A.nlc + lc) * 2 + 1] = (float)hi;
+    const double pad = 0.003 + A.exptimes[lc];
+    const double lo = t1 - pad, hi = t4 + pad;
     if (hi + 2 * err >= 0.5 * p || lo - 2 * err <= -0.5 * p) flags |= FLAG_WIDE;
+    const int ep = A.epids[lc];
+    const int pb = A.pbids[lc];
+    const int ns = A.nsamples[lc];
+    const double d0 = A.t0[(size_t)pv * A.ldt0 + ep] - A.t_ref;
+    const float d0h = __double2float_rn(d0);
+    const double kk = A.k[(size_t)pv * A.nkc + (A.nkc == A.npb ? pb : 0)];
+    // a non-finite disk integral makes every in-box point NaN, as (istar - I A)/istar does
+    const float is = A.istar32[(size_t)pv * A.npb + pb];
+    float* q = A.lc32 + ((size_t)pv * A.nlc + lc) * LC32;
+    q[LC_FLO] = (float)(lo - err);
+    q[LC_FHI] = (float)(hi + err);
+    q[LC_D0H] = d0h;
+    q[LC_D0L] = __double2float_rn(d0 - (double)d0h);
+    q[LC_LO] = (float)lo;
+    q[LC_HI] = (float)hi;
+    q[LC_K] = (float)kk;
+    q[LC_INV1PK] = (float)(1.0 / (1.0 + kk));
+    q[LC_INVIS] = isfinite(is) ? 1.0f / is : __int_as_float(0x7fc00000);
+    q[LC_EXPT] = (float)A.exptimes[lc];
+    q[LC_INVNS] = 1.0f / (float)ns;
+    q[LC_NS] = __int_as_float(ns);
+    q[LC_PB] = __int_as_float(pb);
+    q[13] = q[14] = q[15] = 0.0f;
   }
   o[14] = __int_as_float(flags);
   o[15] = 0.0f;
-  for (int pb = 0; pb < A.npb; ++pb) {
-    double kk = A.k[(size_t)pv * A.nkc + (A.nkc == A.npb ? pb : 0)];
-    float* q = A.pb32 + ((size_t)pv * A.npb + pb) * 4;
-    q[0] = (float)kk;
-    q[1] = (float)(1.0 / (1.0 + kk));
-    // a non-finite disk integral makes every in-box point NaN, as (istar - I A)/istar does
-    float is = A.istar32[(size_t)pv * A.npb + pb];
-    q[2] = isfinite(is) ? 1.0f / is : __int_as_float(0x7fc00000);
-    q[3] = 0.0f;
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -228,234 +251,264 @@ __global__ void __launch_bounds__(256) flux_f64_kernel(FluxF64Args A) {
 }
 
 // ---------------------------------------------------------------------------
-// Split-precision flux.  A warp owns 128 consecutive points of one pv (4 per
-// lane, float4 stores).  Per point: an FP32 fast test of the phase-folded time
-// against the bounding box widened by a per-pv error bound; candidate points
-// get the exact phase reduction in FP32 pairs (error-free transformations)
-// and the exact box test; in-box points are compacted into a per-warp list
-// and their (point, sample) pairs are spread over the 32 lanes, each lane
-// evaluating one sample (z, table interpolation, area) in FP32; a segmented
-// shuffle reduction sums the samples of each point.  Output F = 1 - deficit.
+// Split-precision flux.  A block owns one pv and loops its 8 warps over warp
+// tiles of 128 consecutive points (4 per lane, float4 loads and stores).  The block
+// first stages the pv's orbit record and its per-light-curve records in
+// shared memory, so the per-point work has no dependent global loads.  A warp
+// tile of one light curve whose time range misses every box copy is written
+// as 1.0 without per-point work.  Otherwise, per point: an FP32 fast test of the phase-folded time against the bounding box
+// widened by the pv's error bound; candidates get the exact phase reduction
+// in FP32 pairs (error-free transformations) and the exact box test; in-box
+// points are compacted into a per-warp list whose (point, sample) pairs are
+// spread over the 32 lanes, each lane evaluating one sample (z, table
+// interpolation, area) in FP32; a segmented shuffle reduction sums the
+// samples of each point.  Output F = 1 - deficit.
 // ---------------------------------------------------------------------------
 constexpr int SPLIT_WARPS = 8;
 constexpr int SPLIT_PTS = 4;                 // points per lane
-constexpr int WARP_TILE = 32 * SPLIT_PTS;    // points per warp
+constexpr int WARP_TILE = 32 * SPLIT_PTS;    // points per warp tile
 
 struct FluxSplitArgs {
   const float2* times_ff;
-  const int32_t *lcids, *pbids, *epids, *nsamples;
-  const double* exptimes;
-  const float *orb32, *box32, *ep32, *pb32, *ldm;
-  int npt, npv, npb, nlc, nep, ng, ldflux;
+  const int32_t* lcids;
+  const float *orb32, *lc32, *ldm;
+  int npt, npv, npb, nlc, ng, ldflux;
   float inv_dg;
   float* flux;
 };
 
+constexpr int LC_SMEM = 64;                  // light-curve records staged in shared memory
+
 struct WarpList {
   float tc[WARP_TILE];
   int lc[WARP_TILE];
-  int slot[WARP_TILE];
   int off[WARP_TILE + 1];
   float acc[WARP_TILE];
-  float res[WARP_TILE];
 };
 
-__device__ __forceinline__ float lens_area_f32(float k, float z) {
-  float kap;
-  return ccia_star<float>(k, z, kap);
+// Per-point path for one warp tile of one pv: fast test, exact reduction of
+// candidates, in-box list, samples spread over lanes.  res[] holds 1.0 on
+// entry and the flux of in-box points on exit.
+__device__ __forceinline__ void split_tile_points(const float* __restrict__ orb, const float* __restrict__ LCR,
+                                                  const float* __restrict__ ldm_pv, int ng, float inv_dg,
+                                                  bool wide, const float* hi, const float* lo, const int* lcv,
+                                                  WarpList& L, int lane, float* res) {
+  const unsigned FULL = 0xffffffffu;
+  const float p_hi = orb[10], p_lo = orb[11], inv_p = orb[12];
+  unsigned cand = 0;
+  float nq[SPLIT_PTS];
+#pragma unroll
+  for (int q = 0; q < SPLIT_PTS; ++q) {
+    nq[q] = 0.0f;
+    if (lcv[q] >= 0) {
+      const float4 f = *reinterpret_cast<const float4*>(LCR + lcv[q] * LC32);  // flo, fhi, d0h, d0l
+      const float sv = hi[q] - f.z;
+      const float n = floorf(fmaf(sv, inv_p, 0.5f));
+      nq[q] = n;
+      const float r = fmaf(-n, p_hi, sv);
+      if (wide || (r >= f.x && r <= f.y)) cand |= 1u << q;
+    }
+  }
+  if (!__ballot_sync(FULL, cand != 0)) return;
+  int nitems = 0;
+  int posq[SPLIT_PTS];
+#pragma unroll
+  for (int q = 0; q < SPLIT_PTS; ++q) {
+    bool in = false;
+    float tcv = 0.0f;
+    if (cand >> q & 1u) {
+      const float* R = LCR + lcv[q] * LC32;
+      const float d0h = R[LC_D0H], d0l = R[LC_D0L];
+      float n = nq[q];
+      // tc = (hi + lo) - (d0h + d0l) - n (p_hi + p_lo), FP32 pairs
+      float s1, e1, q1, e2, s2, e3;
+      two_sum(hi[q], -d0h, s1, e1);
+      two_prod(n, p_hi, q1, e2);
+      two_sum(s1, -q1, s2, e3);
+      float tail = ((e1 + e3) - e2) + (lo[q] - d0l) - n * p_lo;
+      float t = s2 + tail;
+      // the fast epoch estimate can be off by one near phase +-1/2
+      if (t >= 0.5f * p_hi) n += 1.0f;
+      else if (t < -0.5f * p_hi) n -= 1.0f;
+      if (n != nq[q]) {
+        two_prod(n, p_hi, q1, e2);
+        two_sum(s1, -q1, s2, e3);
+        tail = ((e1 + e3) - e2) + (lo[q] - d0l) - n * p_lo;
+        t = s2 + tail;
+      }
+      in = (R[LC_LO] <= t && t <= R[LC_HI]);
+      tcv = t;
+    }
+    const unsigned m = __ballot_sync(FULL, in);
+    posq[q] = -1;
+    if (in) {
+      const int pos = nitems + __popc(m & ((1u << lane) - 1u));
+      L.tc[pos] = tcv;
+      L.lc[pos] = lcv[q];
+      posq[q] = pos;
+    }
+    nitems += __popc(m);
+  }
+  __syncwarp();
+  if (nitems > 0) {
+    // exclusive prefix sum of the sample counts -> L.off
+    int carry = 0;
+    for (int c0 = 0; c0 < nitems; c0 += 32) {
+      const int it = c0 + lane;
+      const int v = (it < nitems) ? __float_as_int(LCR[L.lc[it] * LC32 + LC_NS]) : 0;
+      int incl = v;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int u = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d) incl += u;
+      }
+      if (it < nitems) {
+        L.off[it] = carry + incl - v;
+        L.acc[it] = 0.0f;
+      }
+      carry += __shfl_sync(FULL, incl, 31);
+    }
+    __syncwarp();
+    const int total = carry;
+    for (int f0 = 0; f0 < total; f0 += 32) {
+      const int f = f0 + lane;
+      float d = 0.0f;
+      int item = -1;
+      if (f < total) {
+        int lo_i = 0, hi_i = nitems - 1;   // largest item with off[item] <= f
+        while (lo_i < hi_i) {
+          const int mid = (lo_i + hi_i + 1) >> 1;
+          if (L.off[mid] <= f) lo_i = mid; else hi_i = mid - 1;
+        }
+        item = lo_i;
+        const int smp = f - L.off[item];
+        const float* R = LCR + L.lc[item] * LC32;
+        const float k = R[LC_K];
+        // time_offset = exptime ((isample - 0.5)/ns - 0.5), isample = smp + 1
+        const float t = L.tc[item] + R[LC_EXPT] * fmaf(float(smp) + 0.5f, R[LC_INVNS], -0.5f);
+        const float z = sep_c_f32(t, orb);
+        if (z < 1.0f + k) {
+          const float gg = z * R[LC_INV1PK] * inv_dg;
+          int i = (int)gg;
+          i = min(max(i, 0), ng - 2);
+          const float fr = gg - (float)i;
+          const float* lda = ldm_pv + __float_as_int(R[LC_PB]) * ng;
+          const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
+          float kap;
+          d = fmaf(fr, l1 - l0, l0) * ccia_star<float>(k, z, kap);
+        }
+      }
+      // segmented sum over lanes holding the same item
+#pragma unroll
+      for (int dd = 1; dd < 32; dd <<= 1) {
+        const float dv = __shfl_down_sync(FULL, d, dd);
+        const int iv = __shfl_down_sync(FULL, item, dd);
+        if (lane + dd < 32 && iv == item) d += dv;
+      }
+      const int iprev = __shfl_up_sync(FULL, item, 1);
+      if (item >= 0 && (lane == 0 || iprev != item)) L.acc[item] += d;
+      __syncwarp();
+    }
+#pragma unroll
+    for (int q = 0; q < SPLIT_PTS; ++q) {
+      if (posq[q] >= 0) {
+        const float* R = LCR + lcv[q] * LC32;
+        res[q] = 1.0f - L.acc[posq[q]] * R[LC_INVIS] * R[LC_INVNS];
+      }
+    }
+  }
+  __syncwarp();
 }
 
+// Grid: x = ranges of warp tiles, y/z = parameter vectors.  The block stages
+// its pv's orbit and light-curve records in shared memory; each warp loops
+// over tiles.  A tile whose time range (from the precomputed tile summary)
+// misses every box copy of its light curve is written as 1.0 straight away;
+// other tiles load their times and take the per-point path.
+template <bool LC_IN_SMEM>
 __global__ void __launch_bounds__(SPLIT_WARPS * 32) flux_split_kernel(FluxSplitArgs A) {
   __shared__ WarpList lists[SPLIT_WARPS];
+  __shared__ __align__(16) float recs[ORB32 + (LC_IN_SMEM ? LC_SMEM * LC32 : 0)];
   const unsigned FULL = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int pv = block_pv();
-  const int base = (blockIdx.x * SPLIT_WARPS + warp) * WARP_TILE;
-  if (base >= A.npt || pv >= A.npv) return;  // warp-uniform
-  const int pt0 = base + lane * SPLIT_PTS;
-  const float* o = A.orb32 + (size_t)pv * ORB32;
-  const int flags = __float_as_int(__ldg(o + 14));
+  if (pv >= A.npv) return;  // block-uniform
+  const float* lcg = A.lc32 + (size_t)pv * A.nlc * LC32;
+  if (threadIdx.x < ORB32) recs[threadIdx.x] = __ldg(A.orb32 + (size_t)pv * ORB32 + threadIdx.x);
+  if (LC_IN_SMEM)
+    for (int i = threadIdx.x; i < A.nlc * LC32; i += blockDim.x) recs[ORB32 + i] = __ldg(lcg + i);
+  __syncthreads();
+  const float* orb = recs;
+  const float* LCR = LC_IN_SMEM ? recs + ORB32 : lcg;
+  const int flags = __float_as_int(orb[14]);
+  const bool valid = flags & FLAG_VALID;
+  const bool wide = flags & FLAG_WIDE;
+  const float p_hi = orb[10], inv_p = orb[12];
+  const float* ldm_pv = A.ldm + (size_t)pv * A.npb * A.ng;
   float* row = A.flux + (size_t)pv * A.ldflux;
-  const bool vec = (pt0 + SPLIT_PTS <= A.npt) &&
-                   ((reinterpret_cast<uintptr_t>(row + pt0) & 15) == 0);
-
-  float res[SPLIT_PTS] = {1.0f, 1.0f, 1.0f, 1.0f};
-  if (!(flags & FLAG_VALID)) {
-    for (int q = 0; q < SPLIT_PTS; ++q) res[q] = __int_as_float(0x7fc00000);
-  } else {
-    const float p_hi = __ldg(o + 10), p_lo = __ldg(o + 11), inv_p = __ldg(o + 12), err = __ldg(o + 13);
-    const bool wide = flags & FLAG_WIDE;
-    float hi[SPLIT_PTS], lo[SPLIT_PTS];
-    int lcv[SPLIT_PTS];
-    if (pt0 + SPLIT_PTS <= A.npt && ((reinterpret_cast<uintptr_t>(A.times_ff + pt0) & 15) == 0) &&
-        ((reinterpret_cast<uintptr_t>(A.lcids + pt0) & 15) == 0)) {
-      float4 u = __ldg(reinterpret_cast<const float4*>(A.times_ff + pt0));
-      float4 v = __ldg(reinterpret_cast<const float4*>(A.times_ff + pt0 + 2));
-      int4 l4 = __ldg(reinterpret_cast<const int4*>(A.lcids + pt0));
-      hi[0] = u.x; lo[0] = u.y; hi[1] = u.z; lo[1] = u.w;
-      hi[2] = v.x; lo[2] = v.y; hi[3] = v.z; lo[3] = v.w;
-      lcv[0] = l4.x; lcv[1] = l4.y; lcv[2] = l4.z; lcv[3] = l4.w;
+  const bool row_vec = ((A.ldflux & 3) == 0) && ((reinterpret_cast<uintptr_t>(A.flux) & 15) == 0);
+  const float4* meta = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(A.times_ff) +
+                                                       time_meta_offset(A.npt));
+  WarpList& L = lists[warp];
+  const int ntiles = (A.npt + WARP_TILE - 1) / WARP_TILE;
+  for (int tile = blockIdx.x * SPLIT_WARPS + warp; tile < ntiles; tile += gridDim.x * SPLIT_WARPS) {
+    const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
+    const bool full4 = pt0 + SPLIT_PTS <= A.npt;
+    float res[SPLIT_PTS] = {1.0f, 1.0f, 1.0f, 1.0f};
+    if (!valid) {
+#pragma unroll
+      for (int q = 0; q < SPLIT_PTS; ++q) res[q] = __int_as_float(0x7fc00000);
     } else {
-      for (int q = 0; q < SPLIT_PTS; ++q) {
-        int pt = pt0 + q;
-        if (pt < A.npt) {
-          float2 tt = __ldg(A.times_ff + pt);
-          hi[q] = tt.x; lo[q] = tt.y; lcv[q] = __ldg(A.lcids + pt);
+      // Tile cull: the tile's time range against the box copies around it.
+      // The rounding of t - d0 and of j p is covered by the error bound in
+      // the box (flo, fhi).
+      bool tile_out = false;
+      const float4 tm = __ldg(meta + tile);                 // tmin, tmax, lc
+      const int tlc = __float_as_int(tm.z);
+      if (!wide && tlc >= 0) {
+        const float4 f = *reinterpret_cast<const float4*>(LCR + tlc * LC32);  // flo, fhi, d0h, d0l
+        const float smin = tm.x - f.z, smax = tm.y - f.z;
+        const float j0 = ceilf((smin - f.y) * inv_p);
+        bool hit = false;
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+          const float jj = j0 + (float)dj;
+          hit = hit || (fmaf(jj, p_hi, f.x) <= smax && fmaf(jj, p_hi, f.y) >= smin);
+        }
+        tile_out = !hit;
+      }
+      if (!tile_out) {
+        float hi[SPLIT_PTS], lo[SPLIT_PTS];
+        int lcv[SPLIT_PTS];
+        if (full4 && ((reinterpret_cast<uintptr_t>(A.times_ff + pt0) & 15) == 0) &&
+            ((reinterpret_cast<uintptr_t>(A.lcids + pt0) & 15) == 0)) {
+          const float4 u = __ldg(reinterpret_cast<const float4*>(A.times_ff + pt0));
+          const float4 v = __ldg(reinterpret_cast<const float4*>(A.times_ff + pt0 + 2));
+          const int4 l4 = __ldg(reinterpret_cast<const int4*>(A.lcids + pt0));
+          hi[0] = u.x; lo[0] = u.y; hi[1] = u.z; lo[1] = u.w;
+          hi[2] = v.x; lo[2] = v.y; hi[3] = v.z; lo[3] = v.w;
+          lcv[0] = l4.x; lcv[1] = l4.y; lcv[2] = l4.z; lcv[3] = l4.w;
         } else {
-          hi[q] = 0.0f; lo[q] = 0.0f; lcv[q] = -1;
-        }
-      }
-    }
-    // fast test
-    unsigned cand = 0;
-    float nq[SPLIT_PTS];
 #pragma unroll
-    for (int q = 0; q < SPLIT_PTS; ++q) {
-      nq[q] = 0.0f;
-      if (lcv[q] < 0) continue;
-      const int lc = lcv[q];
-      const int ep = __ldg(A.epids + lc);
-      const float d0h = __ldg(A.ep32 + ((size_t)pv * A.nep + ep) * 2);
-      const float s = hi[q] - d0h;
-      const float n = floorf(fmaf(s, inv_p, 0.5f));
-      nq[q] = n;
-      const float r = fmaf(-n, p_hi, s);
-      const float2 bb = __ldg(reinterpret_cast<const float2*>(A.box32) + (size_t)pv * A.nlc + lc);
-      if (wide || (r >= bb.x - err && r <= bb.y + err)) cand |= 1u << q;
-    }
-    if (__ballot_sync(FULL, cand != 0)) {
-      WarpList& L = lists[warp];
-      int nitems = 0;
-      unsigned inbox = 0;
-#pragma unroll
-      for (int q = 0; q < SPLIT_PTS; ++q) {
-        bool in = false;
-        float tcv = 0.0f;
-        if (cand >> q & 1u) {
-          const int lc = lcv[q];
-          const int ep = __ldg(A.epids + lc);
-          const float d0h = __ldg(A.ep32 + ((size_t)pv * A.nep + ep) * 2);
-          const float d0l = __ldg(A.ep32 + ((size_t)pv * A.nep + ep) * 2 + 1);
-          float n = nq[q];
-          // tc = (hi + lo) - (d0h + d0l) - n (p_hi + p_lo), FP32 pairs
-          float s1, e1, q1, e2, s2, e3;
-          two_sum(hi[q], -d0h, s1, e1);
-          two_prod(n, p_hi, q1, e2);
-          two_sum(s1, -q1, s2, e3);
-          float tail = ((e1 + e3) - e2) + (lo[q] - d0l) - n * p_lo;
-          float t = s2 + tail;
-          // the fast epoch estimate can be off by one near phase +-1/2
-          if (t >= 0.5f * p_hi) { n += 1.0f; }
-          else if (t < -0.5f * p_hi) { n -= 1.0f; }
-          if (n != nq[q]) {
-            two_prod(n, p_hi, q1, e2);
-            two_sum(s1, -q1, s2, e3);
-            tail = ((e1 + e3) - e2) + (lo[q] - d0l) - n * p_lo;
-            t = s2 + tail;
-          }
-          const float2 bb = __ldg(reinterpret_cast<const float2*>(A.box32) + (size_t)pv * A.nlc + lc);
-          in = (bb.x <= t && t <= bb.y);
-          tcv = t;
-        }
-        const unsigned m = __ballot_sync(FULL, in);
-        if (in) {
-          const int pos = nitems + __popc(m & ((1u << lane) - 1u));
-          L.tc[pos] = tcv;
-          L.lc[pos] = lcv[q];
-          L.slot[pos] = lane * SPLIT_PTS + q;
-          inbox |= 1u << q;
-        }
-        nitems += __popc(m);
-      }
-      __syncwarp();
-      if (nitems > 0) {
-        // exclusive prefix sum of the sample counts -> L.off
-        int carry = 0;
-        for (int c0 = 0; c0 < nitems; c0 += 32) {
-          const int it = c0 + lane;
-          const int v = (it < nitems) ? __ldg(A.nsamples + L.lc[it]) : 0;
-          int incl = v;
-#pragma unroll
-          for (int d = 1; d < 32; d <<= 1) {
-            int u = __shfl_up_sync(FULL, incl, d);
-            if (lane >= d) incl += u;
-          }
-          if (it < nitems) {
-            L.off[it] = carry + incl - v;
-            L.acc[it] = 0.0f;
-          }
-          carry += __shfl_sync(FULL, incl, 31);
-        }
-        if (lane == 0) L.off[nitems] = carry;
-        __syncwarp();
-        const int total = carry;
-        float c[10];
-#pragma unroll
-        for (int i = 0; i < 10; ++i) c[i] = __ldg(o + i);
-        for (int f0 = 0; f0 < total; f0 += 32) {
-          const int f = f0 + lane;
-          float d = 0.0f;
-          int item = -1;
-          if (f < total) {
-            // largest item with off[item] <= f
-            int lo_i = 0, hi_i = nitems - 1;
-            while (lo_i < hi_i) {
-              int mid = (lo_i + hi_i + 1) >> 1;
-              if (L.off[mid] <= f) lo_i = mid; else hi_i = mid - 1;
-            }
-            item = lo_i;
-            const int s = f - L.off[item];
-            const int lc = L.lc[item];
-            const int ns = __ldg(A.nsamples + lc);
-            const float ex = (float)__ldg(A.exptimes + lc);
-            const int pb = __ldg(A.pbids + lc);
-            const float4 pbr = __ldg(reinterpret_cast<const float4*>(A.pb32) + (size_t)pv * A.npb + pb);
-            const float k = pbr.x, inv1pk = pbr.y;
-            // time_offset = exptime ((isample - 0.5)/ns - 0.5), isample = s + 1
-            const float t = L.tc[item] + ex * ((float(s) + 0.5f) / float(ns) - 0.5f);
-            const float z = sep_c_f32(t, c);
-            if (z < 1.0f + k) {
-              const float gg = z * inv1pk * A.inv_dg;
-              int i = (int)gg;
-              i = min(max(i, 0), A.ng - 2);
-              const float fr = gg - (float)i;
-              const float* lda = A.ldm + ((size_t)pv * A.npb + pb) * A.ng;
-              const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
-              const float ip = fmaf(fr, l1 - l0, l0);
-              d = ip * lens_area_f32(k, z);
+          for (int q = 0; q < SPLIT_PTS; ++q) {
+            const int pt = pt0 + q;
+            if (pt < A.npt) {
+              const float2 tt = __ldg(A.times_ff + pt);
+              hi[q] = tt.x; lo[q] = tt.y; lcv[q] = __ldg(A.lcids + pt);
+            } else {
+              hi[q] = 0.0f; lo[q] = 0.0f; lcv[q] = -1;
             }
           }
-          // segmented sum over lanes holding the same item
-#pragma unroll
-          for (int dd = 1; dd < 32; dd <<= 1) {
-            const float dv = __shfl_down_sync(FULL, d, dd);
-            const int iv = __shfl_down_sync(FULL, item, dd);
-            if (lane + dd < 32 && iv == item) d += dv;
-          }
-          const int iprev = __shfl_up_sync(FULL, item, 1);
-          if (item >= 0 && (lane == 0 || iprev != item)) L.acc[item] += d;
-          __syncwarp();
         }
-        for (int it = lane; it < nitems; it += 32) {
-          const int lc = L.lc[it];
-          const int pb = __ldg(A.pbids + lc);
-          const float inv_is = __ldg(A.pb32 + ((size_t)pv * A.npb + pb) * 4 + 2);
-          const float ns = (float)__ldg(A.nsamples + lc);
-          L.res[L.slot[it]] = 1.0f - L.acc[it] * inv_is / ns;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int q = 0; q < SPLIT_PTS; ++q)
-          if (inbox >> q & 1u) res[q] = L.res[lane * SPLIT_PTS + q];
+        split_tile_points(orb, LCR, ldm_pv, A.ng, A.inv_dg, wide, hi, lo, lcv, L, lane, res);
       }
-      __syncwarp();
     }
-  }
-  if (vec) {
-    __stcs(reinterpret_cast<float4*>(row + pt0), make_float4(res[0], res[1], res[2], res[3]));
-  } else {
-    for (int q = 0; q < SPLIT_PTS; ++q)
-      if (pt0 + q < A.npt) __stcs(row + pt0 + q, res[q]);
+    if (full4 && row_vec) {
+      __stcs(reinterpret_cast<float4*>(row + pt0), make_float4(res[0], res[1], res[2], res[3]));
+    } else {
+      for (int q = 0; q < SPLIT_PTS; ++q)
+        if (pt0 + q < A.npt) __stcs(row + pt0 + q, res[q]);
+    }
   }
 }
 
@@ -473,11 +526,10 @@ size_t rr_full_f64_workspace_bytes(int npv, int npb, int ng) {
 }
 
 size_t rr_full_split_workspace_bytes(int npv, int npb, int nlc, int nep, int ng) {
+  (void)nep;
   Carve c(nullptr);
   c.take<float>((size_t)npv * ORB32);
-  c.take<float>((size_t)npv * nlc * 2);
-  c.take<float>((size_t)npv * nep * 2);
-  c.take<float>((size_t)npv * npb * 4);
+  c.take<float>((size_t)npv * nlc * LC32);
   c.take<float>((size_t)npv * npb * ng);
   return c.used + 256;
 }
@@ -491,16 +543,14 @@ static int check_common(int npt, int nkc, int npv, int nlc, int npb, int nk, int
 }
 
 struct SplitTables {
-  float *orb, *box, *ep, *pb, *ldm;
+  float *orb, *lc, *ldm;
 };
 
-static SplitTables carve_split(void* ws, int npv, int npb, int nlc, int nep, int ng) {
+static SplitTables carve_split(void* ws, int npv, int npb, int nlc, int ng) {
   Carve cv(ws);
   SplitTables t;
   t.orb = cv.take<float>((size_t)npv * ORB32);
-  t.box = cv.take<float>((size_t)npv * nlc * 2);
-  t.ep = cv.take<float>((size_t)npv * nep * 2);
-  t.pb = cv.take<float>((size_t)npv * npb * 4);
+  t.lc = cv.take<float>((size_t)npv * nlc * LC32);
   t.ldm = cv.take<float>((size_t)npv * npb * ng);
   return t;
 }
@@ -518,7 +568,7 @@ int rr_prepare_f64(const double* k, int nkc, const double* p, const double* a, c
   double* orb = cv.take<double>((size_t)npv * ORB64);
   double* ldm = cv.take<double>((size_t)npv * npb * ng);
   dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-  ldm_kernel<double><<<lg, 128, 0, s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0,
+  ldm_kernel<double><<<lg, 128, ldm_smem_bytes<double>(ng, nz), s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0,
                                         nullptr, ldm);
   OrbitArgs oa{};
   oa.k = k; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w;
@@ -569,10 +619,10 @@ int rr_full_f64(const double* times, int npt, const double* k, int nkc, const do
 
 int rr_prepare_split(double t_ref, double t_absmax, const double* k, int nkc, const double* t0, int ldt0,
                      int nep, const double* p, const double* a, const double* inc, const double* e,
-                     const double* w, int npv, int nlc, int npb, const double* exptimes, const float* ldp,
-                     const float* istar, const float* weights, int nk, int ng, int nz, double dk,
-                     double kmin, double kmax, const double* z_edges, void* workspace,
-                     size_t workspace_bytes, void* stream) {
+                     const double* w, int npv, int nlc, int npb, const int32_t* pbids, const int32_t* epids,
+                     const int32_t* nsamples, const double* exptimes, const float* ldp, const float* istar,
+                     const float* weights, int nk, int ng, int nz, double dk, double kmin, double kmax,
+                     const double* z_edges, void* workspace, size_t workspace_bytes, void* stream) {
   if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
   if (npv < 0 || nlc < 1 || npb < 1 || nk < 2 || ng < 2 || nz < 1 || nz > MAX_NZ || nkc < 1 || nep < 1 ||
       nep > ldt0)
@@ -580,35 +630,41 @@ int rr_prepare_split(double t_ref, double t_absmax, const double* k, int nkc, co
   if (npv == 0) return RR_OK;
   if (workspace_bytes < rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng)) return RR_ERR_WORKSPACE;
   cudaStream_t s = as_stream(stream);
-  SplitTables t = carve_split(workspace, npv, npb, nlc, nep, ng);
+  SplitTables t = carve_split(workspace, npv, npb, nlc, ng);
   dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-  ldm_kernel<float><<<lg, 128, 0, s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0,
-                                       nullptr, t.ldm);
+  ldm_kernel<float><<<lg, 128, ldm_smem_bytes<float>(ng, nz), s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk,
+                                                                   kmin, kmax, z_edges, 0, nullptr, t.ldm);
   OrbitArgs oa{};
   oa.k = k; oa.t0 = t0; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w; oa.exptimes = exptimes;
+  oa.pbids = pbids; oa.epids = epids; oa.nsamples = nsamples;
   oa.nkc = nkc; oa.ldt0 = ldt0; oa.nep = nep; oa.npv = npv; oa.nlc = nlc; oa.npb = npb; oa.nz = nz;
-  oa.ldp = ldp; oa.ldp_is_f32 = 1; oa.orb32 = t.orb; oa.box32 = t.box; oa.ep32 = t.ep; oa.pb32 = t.pb;
+  oa.ldp = ldp; oa.ldp_is_f32 = 1; oa.orb32 = t.orb; oa.lc32 = t.lc;
   oa.istar32 = istar; oa.t_ref = t_ref; oa.t_absmax = t_absmax;
   orbit_kernel<true><<<(npv + 31) / 32, 32, 0, s>>>(oa);
   return check_launch("rr_prepare_split");
 }
 
-int rr_flux_split(const float* times_ff, int npt, const int32_t* lcids, const int32_t* pbids,
-                  const int32_t* epids, const int32_t* nsamples, const double* exptimes, int npv, int nlc,
-                  int npb, int nep, int ng, double dg, const void* workspace, float* flux, int ldflux,
-                  void* stream) {
-  if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || nep < 1 || ldflux < npt) return RR_ERR_ARG;
+int rr_flux_split(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
+                  double dg, const void* workspace, float* flux, int ldflux, void* stream) {
+  if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || ldflux < npt) return RR_ERR_ARG;
   if (npv == 0 || npt == 0) return RR_OK;
-  SplitTables t = carve_split(const_cast<void*>(workspace), npv, npb, nlc, nep, ng);
+  SplitTables t = carve_split(const_cast<void*>(workspace), npv, npb, nlc, ng);
   FluxSplitArgs fa{};
   fa.times_ff = reinterpret_cast<const float2*>(times_ff);
-  fa.lcids = lcids; fa.pbids = pbids; fa.epids = epids; fa.nsamples = nsamples; fa.exptimes = exptimes;
-  fa.orb32 = t.orb; fa.box32 = t.box; fa.ep32 = t.ep; fa.pb32 = t.pb; fa.ldm = t.ldm;
-  fa.npt = npt; fa.npv = npv; fa.npb = npb; fa.nlc = nlc; fa.nep = nep; fa.ng = ng; fa.ldflux = ldflux;
+  fa.lcids = lcids;
+  fa.orb32 = t.orb; fa.lc32 = t.lc; fa.ldm = t.ldm;
+  fa.npt = npt; fa.npv = npv; fa.npb = npb; fa.nlc = nlc; fa.ng = ng; fa.ldflux = ldflux;
   fa.inv_dg = (float)(1.0 / dg); fa.flux = flux;
-  dim3 fg((npt + WARP_TILE * SPLIT_WARPS - 1) / (WARP_TILE * SPLIT_WARPS), npv < 65535 ? npv : 65535,
-          (npv + 65534) / 65535);
-  flux_split_kernel<<<fg, SPLIT_WARPS * 32, 0, as_stream(stream)>>>(fa);
+  // blocks per pv: enough for about 16 blocks per SM, each warp looping over tiles
+  const int ntiles = (npt + WARP_TILE - 1) / WARP_TILE;
+  const int max_bx = (ntiles + SPLIT_WARPS - 1) / SPLIT_WARPS;
+  long long bx = (152LL * 16 + npv - 1) / npv;
+  bx = bx < 1 ? 1 : (bx > max_bx ? max_bx : bx);
+  dim3 fg((unsigned)bx, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
+  if (nlc <= LC_SMEM)
+    flux_split_kernel<true><<<fg, SPLIT_WARPS * 32, 0, as_stream(stream)>>>(fa);
+  else
+    flux_split_kernel<false><<<fg, SPLIT_WARPS * 32, 0, as_stream(stream)>>>(fa);
   return check_launch("rr_flux_split");
 }
 
@@ -625,12 +681,11 @@ int rr_full_split(const float* times_ff, double t_ref, double t_absmax, int npt,
   if (nep < 1 || nep > ldt0) return RR_ERR_ARG;
   if (npv == 0 || npt == 0) return RR_OK;
   if (workspace_bytes < rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng)) return RR_ERR_WORKSPACE;
-  st = rr_prepare_split(t_ref, t_absmax, k, nkc, t0, ldt0, nep, p, a, inc, e, w, npv, nlc, npb, exptimes, ldp,
-                        istar, weights, nk, ng, nz, dk, kmin, kmax, z_edges, workspace, workspace_bytes,
-                        stream);
+  st = rr_prepare_split(t_ref, t_absmax, k, nkc, t0, ldt0, nep, p, a, inc, e, w, npv, nlc, npb, pbids, epids,
+                        nsamples, exptimes, ldp, istar, weights, nk, ng, nz, dk, kmin, kmax, z_edges, workspace,
+                        workspace_bytes, stream);
   if (st) return st;
-  return rr_flux_split(times_ff, npt, lcids, pbids, epids, nsamples, exptimes, npv, nlc, npb, nep, ng, dg,
-                       workspace, flux, ldflux, stream);
+  return rr_flux_split(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, flux, ldflux, stream);
 }
 
 }  // extern "C"

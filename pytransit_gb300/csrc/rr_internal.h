@@ -35,6 +35,22 @@ constexpr int ORB64 = 16;
 // c[0..9], [10] p_hi, [11] p_lo, [12] 1/p, [13] fast-test error bound,
 // [14] flags (int bits), [15] unused.
 constexpr int ORB32 = 16;
+// Per-(pv, light curve) record of the split path (16 floats).
+constexpr int LC32 = 16;
+enum LcField {
+  LC_FLO = 0, LC_FHI = 1,     // fast-test box (widened by the error bound)
+  LC_D0H = 2, LC_D0L = 3,     // t0[pv, epoch of lc] - t_ref as an FP32 pair
+  LC_LO = 4, LC_HI = 5,       // bounding box incl. the 0.003 d + exptime pad
+  LC_K = 6, LC_INV1PK = 7,    // radius ratio of the lc's passband, 1/(1+k)
+  LC_INVIS = 8,               // 1/istar of the passband (NaN if istar is not finite)
+  LC_EXPT = 9, LC_INVNS = 10, // exposure time, 1/nsamples
+  LC_NS = 11, LC_PB = 12      // nsamples, passband (int bits)
+};
+// Points per time tile (one warp, four points per lane).  The FP32-pair time
+// array holds 2 * round_up(npt, 2) floats followed by one float4 per tile:
+// (min hi, max hi, light curve id or -1 as int bits, 0).
+constexpr int TIME_TILE = 128;
+__host__ __device__ inline size_t time_meta_offset(int npt) { return 2 * (((size_t)npt + 1) / 2 * 2); }
 constexpr int FLAG_VALID = 1;
 constexpr int FLAG_WIDE = 2;  // box too close to +-p/2: take the exact path for every point
 

@@ -56,14 +56,40 @@ __global__ void weights_3d_kernel(int nk, double kmin, double kmax, const double
   }
 }
 
-__global__ void time_split_kernel(const double* __restrict__ times, int npt, double t_ref,
-                                  float2* __restrict__ out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= npt) return;
-  double dt = times[i] - t_ref;
-  float hi = __double2float_rn(dt);
-  float lo = __double2float_rn(dt - (double)hi);
-  out[i] = make_float2(hi, lo);
+// One warp per 128-point tile: the FP32-pair times (hi, lo) of t - t_ref and
+// the tile's summary (min and max of hi, its light curve or -1 if mixed),
+// which lets the flux kernel skip tiles far from every transit.
+__global__ void time_split_kernel(const double* __restrict__ times, const int32_t* __restrict__ lcids, int npt,
+                                  double t_ref, float2* __restrict__ out, float4* __restrict__ meta) {
+  const int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int ntiles = (npt + TIME_TILE - 1) / TIME_TILE;
+  if (tile >= ntiles) return;  // warp-uniform
+  float tmin = INFINITY, tmax = -INFINITY;
+  int lc = -2;
+  bool same = true;
+  for (int q = 0; q < 4; ++q) {
+    const int i = tile * TIME_TILE + lane * 4 + q;
+    if (i < npt) {
+      const double dt = times[i] - t_ref;
+      const float hi = __double2float_rn(dt);
+      const float lo = __double2float_rn(dt - (double)hi);
+      out[i] = make_float2(hi, lo);
+      tmin = fminf(tmin, hi);
+      tmax = fmaxf(tmax, hi);
+      const int l = lcids[i];
+      if (lc == -2) lc = l;
+      same = same && (l == lc);
+    }
+  }
+  const unsigned FULL = 0xffffffffu;
+  for (int o = 16; o > 0; o >>= 1) {
+    tmin = fminf(tmin, __shfl_xor_sync(FULL, tmin, o));
+    tmax = fmaxf(tmax, __shfl_xor_sync(FULL, tmax, o));
+  }
+  const int lc0 = __shfl_sync(FULL, lc, 0);
+  same = __all_sync(FULL, same && (lc == -2 || lc == lc0));
+  if (lane == 0) meta[tile] = make_float4(tmin, tmax, __int_as_float(same ? lc0 : -1), 0.0f);
 }
 
 constexpr int MAX_LDPAR = 16;
@@ -144,11 +170,20 @@ int rr_weights_3d(int nk, double kmin, double kmax, const double* ze, int nz, in
   return check_launch("rr_weights_3d");
 }
 
-int rr_time_split(const double* times, int npt, double t_ref, float* times_ff, void* stream) {
-  if (npt < 0 || (npt > 0 && (!times || !times_ff))) return RR_ERR_ARG;
+size_t rr_time_split_floats(int npt) {
+  if (npt < 0) return 0;
+  const size_t ntiles = ((size_t)npt + TIME_TILE - 1) / TIME_TILE;
+  return 2 * (((size_t)npt + 1) / 2 * 2) + 4 * ntiles;
+}
+
+int rr_time_split(const double* times, const int32_t* lcids, int npt, double t_ref, float* times_ff,
+                  void* stream) {
+  if (npt < 0 || (npt > 0 && (!times || !lcids || !times_ff))) return RR_ERR_ARG;
   if (npt == 0) return RR_OK;
-  time_split_kernel<<<(npt + 255) / 256, 256, 0, as_stream(stream)>>>(
-      times, npt, t_ref, reinterpret_cast<float2*>(times_ff));
+  const int ntiles = (npt + TIME_TILE - 1) / TIME_TILE;
+  float4* meta = reinterpret_cast<float4*>(times_ff + 2 * (((size_t)npt + 1) / 2 * 2));
+  time_split_kernel<<<(ntiles * 32 + 255) / 256, 256, 0, as_stream(stream)>>>(
+      times, lcids, npt, t_ref, reinterpret_cast<float2*>(times_ff), meta);
   return check_launch("rr_time_split");
 }
 

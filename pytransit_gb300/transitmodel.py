@@ -129,10 +129,11 @@ class TransitModel:
             tmin = tmax = 0.0
         d['t_ref'] = 0.5 * (tmin + tmax)
         d['t_absmax'] = max(abs(tmax - d['t_ref']), abs(tmin - d['t_ref']))
-        d['times_ff'] = torch.empty((max(self.npt, 1), 2), dtype=torch.float32, device=device)
-        _lib.check(_lib.lib().rr_time_split(_lib.ptr(d['time']), self.npt, d['t_ref'],
-                                            _lib.ptr(d['times_ff']), _lib.stream_ptr(device)),
-                   "rr_time_split")
+        L = _lib.lib()
+        d['times_ff'] = torch.empty(max(int(L.rr_time_split_floats(self.npt)), 4), dtype=torch.float32,
+                                    device=device)
+        _lib.check(L.rr_time_split(_lib.ptr(d['time']), _lib.ptr(d['lcids']), self.npt, d['t_ref'],
+                                   _lib.ptr(d['times_ff']), _lib.stream_ptr(device)), "rr_time_split")
         self._dev = d
         return d
 
