@@ -265,6 +265,8 @@ def main():
     ws64 = torch.empty(L.rr_full_f64_workspace_bytes(npv, npb, ng), dtype=torch.uint8, device=device)
     P = _lib.ptr
     kmin, kmax = float(model.klims[0]), float(model.klims[1])
+    B32, nb = model._basis(device, 2, True)
+    B64, _ = model._basis(device, 2, False)
 
     def step_split(ev=None):
         _lib.check(L.rr_ld_tables_f32(2, P(dev["ldc"]), npv, npb, 2, P(tb["mu"]), nz, P(ldp32), P(ist32), sp))
@@ -272,7 +274,7 @@ def main():
                                       P(dev["p"]), P(dev["a"]), P(dev["i"]), P(dev["e"]), P(dev["w"]), npv, nlc,
                                       npb, P(dd["pbids"]), P(dd["epids"]), P(dd["nsamples"]), P(dd["exptimes"]),
                                       P(ldp32), P(ist32), P(tb["W32"]), nk, ng, nz, model.dk, kmin, kmax,
-                                      P(tb["ze"]), P(ws32), ws32.numel(), sp))
+                                      P(tb["ze"]), P(ws32), ws32.numel(), sp, 2, P(dev["ldc"]), 2, P(B32), nb))
         if ev is not None:
             ev[0].record(stream)
         _lib.check(L.rr_flux_split(P(dd["times_ff"]), npt, P(dd["lcids"]), npv, nlc, npb, ng, model.dg,
@@ -282,11 +284,12 @@ def main():
 
     def step_fp64():
         _lib.check(L.rr_ld_tables_f64(2, P(dev["ldc"]), npv, npb, 2, P(tb["mu"]), nz, P(ldp64), P(ist64), sp))
-        _lib.check(L.rr_full_f64(P(dd["time"]), npt, P(dev["k"]), 1, P(dev["t0"]), 1, P(dev["p"]), P(dev["a"]),
-                                 P(dev["i"]), P(dev["e"]), P(dev["w"]), npv, nlc, npb, P(dd["lcids"]),
-                                 P(dd["pbids"]), P(dd["epids"]), P(dd["nsamples"]), P(dd["exptimes"]), P(ldp64),
-                                 P(ist64), P(tb["W64"]), nk, ng, nz, model.dk, kmin, kmax, model.dg, P(tb["ze"]),
-                                 P(ws64), ws64.numel(), P(flux64), npt, sp))
+        _lib.check(L.rr_prepare_f64(P(dev["k"]), 1, P(dev["p"]), P(dev["a"]), P(dev["i"]), P(dev["e"]),
+                                    P(dev["w"]), npv, npb, P(ldp64), P(tb["W64"]), nk, ng, nz, model.dk, kmin, kmax,
+                                    P(tb["ze"]), P(ws64), ws64.numel(), sp, 2, P(dev["ldc"]), 2, P(B64), nb))
+        _lib.check(L.rr_flux_f64(P(dd["time"]), npt, P(dev["k"]), 1, P(dev["t0"]), 1, P(dev["p"]), npv, nlc, npb,
+                                 P(dd["lcids"]), P(dd["pbids"]), P(dd["epids"]), P(dd["nsamples"]),
+                                 P(dd["exptimes"]), P(ist64), ng, model.dg, P(ws64), P(flux64), npt, sp))
 
     def timed(fn, steps, warmup, per_step_events=False):
         for _ in range(warmup):

@@ -120,13 +120,25 @@ int rr_full_split(const float *times_ff, double t_ref, double t_absmax, int npt,
                   double kmin, double kmax, double dg, const double *z_edges, void *workspace,
                   size_t workspace_bytes, float *flux, int ldflux, void *stream);
 
+/* Affine LD laws (all named laws except power-2 and power-2-pm) are
+ * I(mu) = sum_b coef_b phi_b(mu); their LD means need only the per-k-row
+ * basis tables B[nk, nb, ng] = W @ phi_b (nb = rr_basis_count(law, npar), 0
+ * for the other laws), built once per model by rr_basis_tables (B32 may be
+ * NULL).  Passing them to rr_prepare_* (law, ldc[npv, npb, npar], basis, nb)
+ * replaces the per-pv W @ ldp products of model_full.py:46-51; basis = NULL
+ * selects the generic products. */
+int rr_basis_count(int law, int npar);
+int rr_basis_tables(int law, int npar, const double *mu, int nz, const double *W64, int nk, int ng,
+                    double *B64, float *B32, void *stream);
+
 /* The two stages of rr_full_f64, callable separately (the workspace carries
  * the per-parameter-vector tables from one to the other): the prologue of
  * model_full.py:39-71 and the flux loop of model_full.py:75-99. */
 int rr_prepare_f64(const double *k, int nkc, const double *p, const double *a, const double *inc,
                    const double *e, const double *w, int npv, int npb, const double *ldp,
                    const double *weights, int nk, int ng, int nz, double dk, double kmin, double kmax,
-                   const double *z_edges, void *workspace, size_t workspace_bytes, void *stream);
+                   const double *z_edges, void *workspace, size_t workspace_bytes, void *stream,
+                   int law, const double *ldc, int npar, const double *basis, int nb);
 int rr_flux_f64(const double *times, int npt, const double *k, int nkc, const double *t0, int ldt0,
                 const double *p, int npv, int nlc, int npb, const int32_t *lcids, const int32_t *pbids,
                 const int32_t *epids, const int32_t *nsamples, const double *exptimes,
@@ -142,7 +154,8 @@ int rr_prepare_split(double t_ref, double t_absmax, const double *k, int nkc, co
                      const int32_t *epids, const int32_t *nsamples, const double *exptimes,
                      const float *ldp, const float *istar, const float *weights, int nk, int ng, int nz,
                      double dk, double kmin, double kmax, const double *z_edges, void *workspace,
-                     size_t workspace_bytes, void *stream);
+                     size_t workspace_bytes, void *stream, int law, const double *ldc, int npar,
+                     const float *basis, int nb);
 int rr_flux_split(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb, int ng,
                   double dg, const void *workspace, float *flux, int ldflux, void *stream);
 

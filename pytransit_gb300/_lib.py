@@ -44,11 +44,14 @@ def _sig(L):
                                  _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d,
                                  _d, _d, _vp, _vp, _sz, _vp, _i, _vp])
     L.rr_prepare_f64.argtypes = ([_vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _i, _i, _d, _d, _d,
-                                  _vp, _vp, _sz, _vp])
+                                  _vp, _vp, _sz, _vp, _i, _vp, _i, _vp, _i])
+    L.rr_basis_count.argtypes = [_i, _i]
+    L.rr_basis_tables.argtypes = [_i, _i, _vp, _i, _vp, _i, _i, _vp, _vp, _vp]
     L.rr_flux_f64.argtypes = ([_vp, _i, _vp, _i, _vp, _i, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i,
                                _d, _vp, _vp, _i, _vp])
     L.rr_prepare_split.argtypes = ([_d, _d, _vp, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp,
-                                    _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _vp, _vp, _sz, _vp])
+                                    _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _vp, _vp, _sz, _vp,
+                                    _i, _vp, _i, _vp, _i])
     L.rr_flux_split.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _vp, _i, _vp]
     for name, args in _EXTRA_SIGNATURES.items():
         if hasattr(L, name):

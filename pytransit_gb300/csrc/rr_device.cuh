@@ -231,6 +231,61 @@ __device__ inline bool ld_dintegral(int law, const R* pv, int j, R& d) {
 }
 
 // ---------------------------------------------------------------------------
+// Affine laws.  Every named law except power-2 and power-2-pm is
+// I(mu) = sum_b coef_b phi_b(mu) with fixed basis functions phi_b, so the LD
+// means reduce to sum_b coef_b (W @ phi_b): per-k-row basis tables replace the
+// per-pv matrix-vector products.  basis_count returns 0 for the other laws.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline int basis_count(int law, int npar) {
+  switch (law) {
+    case LD_UNIFORM: return 1;
+    case LD_LINEAR: return 2;
+    case LD_QUADRATIC: case LD_QUADRATIC_TRI: case LD_SQUARE_ROOT: case LD_LOGARITHMIC: case LD_EXPONENTIAL:
+      return 3;
+    case LD_NONLINEAR: return 5;
+    case LD_GENERAL: return npar;
+  }
+  return 0;
+}
+
+__device__ inline double basis_value(int law, int b, double mu) {
+  if (law == LD_GENERAL) return 1.0 - pow(mu, (double)(b + 1));
+  if (b == 0) return 1.0;
+  switch (law) {
+    case LD_LINEAR: return -(1.0 - mu);
+    case LD_QUADRATIC: case LD_QUADRATIC_TRI: return b == 1 ? -(1.0 - mu) : -(1.0 - mu) * (1.0 - mu);
+    case LD_NONLINEAR:
+      switch (b) {
+        case 1: return -(1.0 - sqrt(mu));
+        case 2: return -(1.0 - mu);
+        case 3: return -(1.0 - pow(mu, 1.5));
+        default: return -(1.0 - mu * mu);
+      }
+    case LD_SQUARE_ROOT: return b == 1 ? -(1.0 - mu) : -(1.0 - sqrt(mu));
+    case LD_LOGARITHMIC: return b == 1 ? -(1.0 - mu) : -mu * log(mu);
+    case LD_EXPONENTIAL: return b == 1 ? -(1.0 - mu) : -1.0 / (1.0 - exp(mu));
+  }
+  return 0.0;
+}
+
+// coef[b] of one parameter vector's coefficients pv[npar]
+__device__ inline void basis_coefs(int law, const double* pv, int npar, double* coef) {
+  switch (law) {
+    case LD_GENERAL:
+      for (int i = 0; i < npar; ++i) coef[i] = pv[i];
+      return;
+    case LD_QUADRATIC_TRI: {
+      double a = sqrt(pv[0]), b = 2 * pv[1];
+      coef[0] = 1.0; coef[1] = a * b; coef[2] = a * (1. - b);
+      return;
+    }
+    default:
+      coef[0] = 1.0;
+      for (int i = 1; i < basis_count(law, npar); ++i) coef[i] = pv[i - 1];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Orbit layer: Taylor coefficients of the sky position about conjunction
 // ---------------------------------------------------------------------------
 

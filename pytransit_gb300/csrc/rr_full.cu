@@ -95,6 +95,103 @@ static size_t ldm_smem_bytes(int ng, int nz) {
 }
 
 // ---------------------------------------------------------------------------
+// Basis tables of an affine law: B[ik][b][g] = sum_z W[ik][g][z] phi_b(mu_z),
+// one thread per (ik, g), FP64 (and an FP32 copy).
+// ---------------------------------------------------------------------------
+__global__ void basis_tables_kernel(int law, int nb, const double* __restrict__ mu, int nz,
+                                    const double* __restrict__ W, int nk, int ng, double* __restrict__ B64,
+                                    float* __restrict__ B32) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= nk * ng) return;
+  const int ik = row / ng, g = row % ng;
+  const double* w = W + (size_t)row * nz;
+  for (int b = 0; b < nb; ++b) {
+    double acc = 0.0;
+    for (int z = 0; z < nz; ++z) acc += w[z] * basis_value(law, b, mu[z]);
+    const size_t o = ((size_t)ik * nb + b) * ng + g;
+    B64[o] = acc;
+    if (B32) B32[o] = (float)acc;
+  }
+}
+
+// LD means of an affine law from the basis tables, one block per pv:
+//   ldm[pv, pb, g] = sum_b coef_b(pv, pb) ((1-ak) B[ik][b][g] + ak B[ik+1][b][g]),
+// k, ik, ak as model_full.py:46-51.  Outside the 3D table (k outside
+// [kmin, kmax], or ik+1 == nk) the 2D table at k is built row by row in FP64
+// and applied to ldp, as the generic kernel does.
+constexpr int MAX_BASIS = 16;
+
+template <typename R>
+__global__ void __launch_bounds__(128)
+ldm_basis_kernel(int law, const double* __restrict__ ldc, int npar, int npb, const double* __restrict__ kw,
+                 int kw_stride, const R* __restrict__ B, int nb, int nk, int ng, double dk, double kmin,
+                 double kmax, const R* __restrict__ ldp, int nz, const double* __restrict__ ze,
+                 R* __restrict__ ldm) {
+  extern __shared__ __align__(16) unsigned char bsm[];
+  R* coef = reinterpret_cast<R*>(bsm);                    // [npb][nb]
+  __shared__ int s_ik;
+  __shared__ double s_ak;
+  const int pv = blockIdx.x;
+  if (threadIdx.x == 0) {
+    const double k = kw[(size_t)pv * kw_stride];
+    int ik = -1;
+    double ak = 0.0;
+    if (kmin <= k && k <= kmax) {
+      ik = (int)floor((k - kmin) / dk);
+      ak = (k - kmin - ik * dk) / dk;
+      if (ik + 1 >= nk || ik < 0) ik = -1;
+    }
+    s_ik = ik;
+    s_ak = ak;
+  }
+  for (int pb = threadIdx.x; pb < npb; pb += blockDim.x) {
+    double c[MAX_BASIS];
+    basis_coefs(law, ldc + ((size_t)pv * npb + pb) * npar, npar, c);
+    for (int b = 0; b < nb; ++b) coef[pb * nb + b] = (R)c[b];
+  }
+  __syncthreads();
+  const int ik = s_ik;
+  R* out = ldm + (size_t)pv * npb * ng;
+  if (ik >= 0) {
+    const R a1 = (R)s_ak, a0 = R(1) - (R)s_ak;
+    const R* B0 = B + (size_t)ik * nb * ng;
+    const R* B1 = B0 + (size_t)nb * ng;
+    for (int j = threadIdx.x; j < npb * ng; j += blockDim.x) {
+      const int pb = j / ng, g = j % ng;
+      R d0 = R(0), d1 = R(0);
+      for (int b = 0; b < nb; ++b) {
+        d0 += coef[pb * nb + b] * __ldg(B0 + b * ng + g);
+        d1 += coef[pb * nb + b] * __ldg(B1 + b * ng + g);
+      }
+      out[j] = a0 * d0 + a1 * d1;
+    }
+  } else {
+    const double k = kw[(size_t)pv * kw_stride];
+    const double gstep = (1.0 - 1e-7) / (double)(ng - 1);
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+      double gg = (double)g * gstep;
+      if (g == ng - 1) gg = 1.0 - 1e-7;
+      const double bb = gg * (1.0 + k);
+      double w[64];
+      double a0 = cci_acos(ze[0], k, bb), s = a0;
+      w[0] = a0;
+      for (int z = 1; z < nz; ++z) {
+        const double a1 = cci_acos(ze[z], k, bb);
+        w[z] = a1 - a0;
+        a0 = a1;
+        s += w[z];
+      }
+      for (int pb = 0; pb < npb; ++pb) {
+        const R* l = ldp + ((size_t)pv * npb + pb) * nz;
+        double acc = 0.0;
+        for (int z = 0; z < nz; ++z) acc += (w[z] / s) * (double)l[z];
+        out[(size_t)pb * ng + g] = (R)acc;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Orbit prologue, model_full.py:39-42 and 56-71, one thread per pv:
 // validity, Taylor coefficients (solve2d), contact points (bounding_box).
 // ---------------------------------------------------------------------------
@@ -286,135 +383,192 @@ struct WarpList {
   float acc[WARP_TILE];
 };
 
-// Per-point path for one warp tile of one pv: fast test, exact reduction of
-// candidates, in-box list, samples spread over lanes.  res[] holds 1.0 on
-// entry and the flux of in-box points on exit.
+// Exact phase-folded time of one point from its FP32-pair time (hi, lo) and
+// the light-curve record (t0 - t_ref pair), starting from the epoch estimate
+// n: tc = (hi + lo) - (d0h + d0l) - n (p_hi + p_lo) with error-free
+// transformations; n is corrected once if the estimate was one off.
+__device__ __forceinline__ float exact_tc_pair(float hi, float lo, float d0h, float d0l, float n, float p_hi,
+                                               float p_lo, float& tail) {
+  float s1, e1, q1, e2, s2, e3;
+  two_sum(hi, -d0h, s1, e1);
+  two_prod(n, p_hi, q1, e2);
+  two_sum(s1, -q1, s2, e3);
+  tail = ((e1 + e3) - e2) + (lo - d0l) - n * p_lo;
+  float t = s2 + tail;
+  if (t >= 0.5f * p_hi || t < -0.5f * p_hi) {
+    n += (t >= 0.5f * p_hi) ? 1.0f : -1.0f;
+    two_prod(n, p_hi, q1, e2);
+    two_sum(s1, -q1, s2, e3);
+    tail = ((e1 + e3) - e2) + (lo - d0l) - n * p_lo;
+  }
+  return s2;   // tc = s2 + tail
+}
+
+__device__ __forceinline__ float exact_tc(float hi, float lo, float d0h, float d0l, float n, float p_hi,
+                                          float p_lo) {
+  float tail;
+  const float s2 = exact_tc_pair(hi, lo, d0h, d0l, n, p_hi, p_lo, tail);
+  return s2 + tail;
+}
+
+// Per-point path for one warp tile of one pv.  Phase-folded times: for a tile
+// of one light curve whose span plus box half-width is below p/2, the exact time of the tile's
+// first point plus each point's (exact, small) offset from it; otherwise a
+// fast FP32 test per point and the exact reduction for candidates.  Then the
+// samples of the in-box points: one lane per point when every in-box point
+// has one sample, else a per-warp list whose (point, sample) pairs are spread
+// over the lanes and summed with a segmented shuffle reduction.  res[] holds
+// 1.0 on entry and the flux of in-box points on exit.
 __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb, const float* __restrict__ LCR,
                                                   const float* __restrict__ ldm_pv, int ng, float inv_dg,
-                                                  bool wide, const float* hi, const float* lo, const int* lcv,
-                                                  WarpList& L, int lane, float* res) {
+                                                  bool wide, float4 tm, const float* hi, const float* lo,
+                                                  const int* lcv, WarpList& L, int lane, float* res) {
   const unsigned FULL = 0xffffffffu;
   const float p_hi = orb[10], p_lo = orb[11], inv_p = orb[12];
-  unsigned cand = 0;
-  float nq[SPLIT_PTS];
+  const int tlc = __float_as_int(tm.z);
+  float tcq[SPLIT_PTS];
+  unsigned inb = 0;
+  // Tile-relative times are exact whenever no point of the tile can fold onto
+  // another box copy: span + |box| < p/2 (points whose offset crosses p/2 are
+  // then out of box in both foldings).
+  const float* RT = LCR + (tlc >= 0 ? tlc : 0) * LC32;
+  if (!wide && tlc >= 0 && (tm.y - tm.x) + fmaxf(-RT[LC_LO], RT[LC_HI]) < 0.5f * p_hi) {
+    const float* R = RT;
+    const float h0 = __shfl_sync(FULL, hi[0], 0), l0 = __shfl_sync(FULL, lo[0], 0);
+    const float n0 = floorf(fmaf(h0 - R[LC_D0H], inv_p, 0.5f));
+    float tail0;
+    const float s0 = exact_tc_pair(h0, l0, R[LC_D0H], R[LC_D0L], n0, p_hi, p_lo, tail0);
+    const float blo = R[LC_LO], bhi = R[LC_HI];
 #pragma unroll
-  for (int q = 0; q < SPLIT_PTS; ++q) {
-    nq[q] = 0.0f;
-    if (lcv[q] >= 0) {
+    for (int q = 0; q < SPLIT_PTS; ++q) {
+      // s0 + (hi - h0) is exact (Sterbenz) near the transit, where the two
+      // nearly cancel; the small terms go in last: one rounding at |tc| scale
+      tcq[q] = (s0 + (hi[q] - h0)) + ((lo[q] - l0) + tail0);
+      if (lcv[q] >= 0 && blo <= tcq[q] && tcq[q] <= bhi) inb |= 1u << q;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < SPLIT_PTS; ++q) {
+      tcq[q] = 0.0f;
+      if (lcv[q] < 0) continue;
       const float4 f = *reinterpret_cast<const float4*>(LCR + lcv[q] * LC32);  // flo, fhi, d0h, d0l
       const float sv = hi[q] - f.z;
       const float n = floorf(fmaf(sv, inv_p, 0.5f));
-      nq[q] = n;
       const float r = fmaf(-n, p_hi, sv);
-      if (wide || (r >= f.x && r <= f.y)) cand |= 1u << q;
+      if (wide || (r >= f.x && r <= f.y)) {
+        const float t = exact_tc(hi[q], lo[q], f.z, f.w, n, p_hi, p_lo);
+        const float* R = LCR + lcv[q] * LC32;
+        tcq[q] = t;
+        if (R[LC_LO] <= t && t <= R[LC_HI]) inb |= 1u << q;
+      }
     }
   }
-  if (!__ballot_sync(FULL, cand != 0)) return;
+  if (!__ballot_sync(FULL, inb != 0)) return;
+  bool single = true;
+#pragma unroll
+  for (int q = 0; q < SPLIT_PTS; ++q)
+    if (inb >> q & 1u) single = single && (__float_as_int(LCR[lcv[q] * LC32 + LC_NS]) == 1);
+  if (__all_sync(FULL, single)) {
+#pragma unroll
+    for (int q = 0; q < SPLIT_PTS; ++q) {
+      if (!(inb >> q & 1u)) continue;
+      const float* R = LCR + lcv[q] * LC32;
+      const float k = R[LC_K];
+      const float z = sep_c_f32(tcq[q], orb);
+      float d = 0.0f;
+      if (z < 1.0f + k) {
+        const float gg = z * R[LC_INV1PK] * inv_dg;
+        int i = (int)gg;
+        i = min(max(i, 0), ng - 2);
+        const float fr = gg - (float)i;
+        const float* lda = ldm_pv + __float_as_int(R[LC_PB]) * ng;
+        const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
+        float kap;
+        d = fmaf(fr, l1 - l0, l0) * ccia_star<float>(k, z, kap);
+      }
+      res[q] = 1.0f - d * R[LC_INVIS];
+    }
+    return;
+  }
   int nitems = 0;
   int posq[SPLIT_PTS];
 #pragma unroll
   for (int q = 0; q < SPLIT_PTS; ++q) {
-    bool in = false;
-    float tcv = 0.0f;
-    if (cand >> q & 1u) {
-      const float* R = LCR + lcv[q] * LC32;
-      const float d0h = R[LC_D0H], d0l = R[LC_D0L];
-      float n = nq[q];
-      // tc = (hi + lo) - (d0h + d0l) - n (p_hi + p_lo), FP32 pairs
-      float s1, e1, q1, e2, s2, e3;
-      two_sum(hi[q], -d0h, s1, e1);
-      two_prod(n, p_hi, q1, e2);
-      two_sum(s1, -q1, s2, e3);
-      float tail = ((e1 + e3) - e2) + (lo[q] - d0l) - n * p_lo;
-      float t = s2 + tail;
-      // the fast epoch estimate can be off by one near phase +-1/2
-      if (t >= 0.5f * p_hi) n += 1.0f;
-      else if (t < -0.5f * p_hi) n -= 1.0f;
-      if (n != nq[q]) {
-        two_prod(n, p_hi, q1, e2);
-        two_sum(s1, -q1, s2, e3);
-        tail = ((e1 + e3) - e2) + (lo[q] - d0l) - n * p_lo;
-        t = s2 + tail;
-      }
-      in = (R[LC_LO] <= t && t <= R[LC_HI]);
-      tcv = t;
-    }
+    const bool in = inb >> q & 1u;
     const unsigned m = __ballot_sync(FULL, in);
     posq[q] = -1;
     if (in) {
       const int pos = nitems + __popc(m & ((1u << lane) - 1u));
-      L.tc[pos] = tcv;
+      L.tc[pos] = tcq[q];
       L.lc[pos] = lcv[q];
       posq[q] = pos;
     }
     nitems += __popc(m);
   }
   __syncwarp();
-  if (nitems > 0) {
-    // exclusive prefix sum of the sample counts -> L.off
-    int carry = 0;
-    for (int c0 = 0; c0 < nitems; c0 += 32) {
-      const int it = c0 + lane;
-      const int v = (it < nitems) ? __float_as_int(LCR[L.lc[it] * LC32 + LC_NS]) : 0;
-      int incl = v;
+  // exclusive prefix sum of the sample counts -> L.off
+  int carry = 0;
+  for (int c0 = 0; c0 < nitems; c0 += 32) {
+    const int it = c0 + lane;
+    const int v = (it < nitems) ? __float_as_int(LCR[L.lc[it] * LC32 + LC_NS]) : 0;
+    int incl = v;
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const int u = __shfl_up_sync(FULL, incl, d);
-        if (lane >= d) incl += u;
-      }
-      if (it < nitems) {
-        L.off[it] = carry + incl - v;
-        L.acc[it] = 0.0f;
-      }
-      carry += __shfl_sync(FULL, incl, 31);
+    for (int d = 1; d < 32; d <<= 1) {
+      const int u = __shfl_up_sync(FULL, incl, d);
+      if (lane >= d) incl += u;
     }
+    if (it < nitems) {
+      L.off[it] = carry + incl - v;
+      L.acc[it] = 0.0f;
+    }
+    carry += __shfl_sync(FULL, incl, 31);
+  }
+  __syncwarp();
+  const int total = carry;
+  for (int f0 = 0; f0 < total; f0 += 32) {
+    const int f = f0 + lane;
+    float d = 0.0f;
+    int item = -1;
+    if (f < total) {
+      int lo_i = 0, hi_i = nitems - 1;   // largest item with off[item] <= f
+      while (lo_i < hi_i) {
+        const int mid = (lo_i + hi_i + 1) >> 1;
+        if (L.off[mid] <= f) lo_i = mid; else hi_i = mid - 1;
+      }
+      item = lo_i;
+      const int smp = f - L.off[item];
+      const float* R = LCR + L.lc[item] * LC32;
+      const float k = R[LC_K];
+      // time_offset = exptime ((isample - 0.5)/ns - 0.5), isample = smp + 1
+      const float t = L.tc[item] + R[LC_EXPT] * fmaf(float(smp) + 0.5f, R[LC_INVNS], -0.5f);
+      const float z = sep_c_f32(t, orb);
+      if (z < 1.0f + k) {
+        const float gg = z * R[LC_INV1PK] * inv_dg;
+        int i = (int)gg;
+        i = min(max(i, 0), ng - 2);
+        const float fr = gg - (float)i;
+        const float* lda = ldm_pv + __float_as_int(R[LC_PB]) * ng;
+        const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
+        float kap;
+        d = fmaf(fr, l1 - l0, l0) * ccia_star<float>(k, z, kap);
+      }
+    }
+    // segmented sum over lanes holding the same item
+#pragma unroll
+    for (int dd = 1; dd < 32; dd <<= 1) {
+      const float dv = __shfl_down_sync(FULL, d, dd);
+      const int iv = __shfl_down_sync(FULL, item, dd);
+      if (lane + dd < 32 && iv == item) d += dv;
+    }
+    const int iprev = __shfl_up_sync(FULL, item, 1);
+    if (item >= 0 && (lane == 0 || iprev != item)) L.acc[item] += d;
     __syncwarp();
-    const int total = carry;
-    for (int f0 = 0; f0 < total; f0 += 32) {
-      const int f = f0 + lane;
-      float d = 0.0f;
-      int item = -1;
-      if (f < total) {
-        int lo_i = 0, hi_i = nitems - 1;   // largest item with off[item] <= f
-        while (lo_i < hi_i) {
-          const int mid = (lo_i + hi_i + 1) >> 1;
-          if (L.off[mid] <= f) lo_i = mid; else hi_i = mid - 1;
-        }
-        item = lo_i;
-        const int smp = f - L.off[item];
-        const float* R = LCR + L.lc[item] * LC32;
-        const float k = R[LC_K];
-        // time_offset = exptime ((isample - 0.5)/ns - 0.5), isample = smp + 1
-        const float t = L.tc[item] + R[LC_EXPT] * fmaf(float(smp) + 0.5f, R[LC_INVNS], -0.5f);
-        const float z = sep_c_f32(t, orb);
-        if (z < 1.0f + k) {
-          const float gg = z * R[LC_INV1PK] * inv_dg;
-          int i = (int)gg;
-          i = min(max(i, 0), ng - 2);
-          const float fr = gg - (float)i;
-          const float* lda = ldm_pv + __float_as_int(R[LC_PB]) * ng;
-          const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
-          float kap;
-          d = fmaf(fr, l1 - l0, l0) * ccia_star<float>(k, z, kap);
-        }
-      }
-      // segmented sum over lanes holding the same item
+  }
 #pragma unroll
-      for (int dd = 1; dd < 32; dd <<= 1) {
-        const float dv = __shfl_down_sync(FULL, d, dd);
-        const int iv = __shfl_down_sync(FULL, item, dd);
-        if (lane + dd < 32 && iv == item) d += dv;
-      }
-      const int iprev = __shfl_up_sync(FULL, item, 1);
-      if (item >= 0 && (lane == 0 || iprev != item)) L.acc[item] += d;
-      __syncwarp();
-    }
-#pragma unroll
-    for (int q = 0; q < SPLIT_PTS; ++q) {
-      if (posq[q] >= 0) {
-        const float* R = LCR + lcv[q] * LC32;
-        res[q] = 1.0f - L.acc[posq[q]] * R[LC_INVIS] * R[LC_INVNS];
-      }
+  for (int q = 0; q < SPLIT_PTS; ++q) {
+    if (posq[q] >= 0) {
+      const float* R = LCR + lcv[q] * LC32;
+      res[q] = 1.0f - L.acc[posq[q]] * R[LC_INVIS] * R[LC_INVNS];
     }
   }
   __syncwarp();
@@ -500,7 +654,7 @@ __global__ void __launch_bounds__(SPLIT_WARPS * 32) flux_split_kernel(FluxSplitA
             }
           }
         }
-        split_tile_points(orb, LCR, ldm_pv, A.ng, A.inv_dg, wide, hi, lo, lcv, L, lane, res);
+        split_tile_points(orb, LCR, ldm_pv, A.ng, A.inv_dg, wide, tm, hi, lo, lcv, L, lane, res);
       }
     }
     if (full4 && row_vec) {
@@ -558,7 +712,8 @@ static SplitTables carve_split(void* ws, int npv, int npb, int nlc, int ng) {
 int rr_prepare_f64(const double* k, int nkc, const double* p, const double* a, const double* inc,
                    const double* e, const double* w, int npv, int npb, const double* ldp,
                    const double* weights, int nk, int ng, int nz, double dk, double kmin, double kmax,
-                   const double* z_edges, void* workspace, size_t workspace_bytes, void* stream) {
+                   const double* z_edges, void* workspace, size_t workspace_bytes, void* stream,
+                   int law, const double* ldc, int npar, const double* basis, int nb) {
   if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
   if (npv < 0 || npb < 1 || nk < 2 || ng < 2 || nz < 1 || nz > MAX_NZ || nkc < 1) return RR_ERR_ARG;
   if (npv == 0) return RR_OK;
@@ -567,9 +722,14 @@ int rr_prepare_f64(const double* k, int nkc, const double* p, const double* a, c
   Carve cv(workspace);
   double* orb = cv.take<double>((size_t)npv * ORB64);
   double* ldm = cv.take<double>((size_t)npv * npb * ng);
-  dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-  ldm_kernel<double><<<lg, 128, ldm_smem_bytes<double>(ng, nz), s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0,
-                                        nullptr, ldm);
+  if (basis && nb > 0 && nb <= MAX_BASIS && ldc) {
+    ldm_basis_kernel<double><<<npv, 128, sizeof(double) * npb * nb, s>>>(
+        law, ldc, npar, npb, k, nkc, basis, nb, nk, ng, dk, kmin, kmax, ldp, nz, z_edges, ldm);
+  } else {
+    dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
+    ldm_kernel<double><<<lg, 128, ldm_smem_bytes<double>(ng, nz), s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk,
+                                                                       kmin, kmax, z_edges, 0, nullptr, ldm);
+  }
   OrbitArgs oa{};
   oa.k = k; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w;
   oa.nkc = nkc; oa.npv = npv; oa.npb = npb; oa.nz = nz;
@@ -611,7 +771,7 @@ int rr_full_f64(const double* times, int npt, const double* k, int nkc, const do
   if (npv == 0 || npt == 0) return RR_OK;
   if (workspace_bytes < rr_full_f64_workspace_bytes(npv, npb, ng)) return RR_ERR_WORKSPACE;
   st = rr_prepare_f64(k, nkc, p, a, inc, e, w, npv, npb, ldp, weights, nk, ng, nz, dk, kmin, kmax, z_edges,
-                      workspace, workspace_bytes, stream);
+                      workspace, workspace_bytes, stream, 0, nullptr, 0, nullptr, 0);
   if (st) return st;
   return rr_flux_f64(times, npt, k, nkc, t0, ldt0, p, npv, nlc, npb, lcids, pbids, epids, nsamples, exptimes,
                      istar, ng, dg, workspace, flux, ldflux, stream);
@@ -622,7 +782,8 @@ int rr_prepare_split(double t_ref, double t_absmax, const double* k, int nkc, co
                      const double* w, int npv, int nlc, int npb, const int32_t* pbids, const int32_t* epids,
                      const int32_t* nsamples, const double* exptimes, const float* ldp, const float* istar,
                      const float* weights, int nk, int ng, int nz, double dk, double kmin, double kmax,
-                     const double* z_edges, void* workspace, size_t workspace_bytes, void* stream) {
+                     const double* z_edges, void* workspace, size_t workspace_bytes, void* stream, int law,
+                     const double* ldc, int npar, const float* basis, int nb) {
   if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
   if (npv < 0 || nlc < 1 || npb < 1 || nk < 2 || ng < 2 || nz < 1 || nz > MAX_NZ || nkc < 1 || nep < 1 ||
       nep > ldt0)
@@ -631,9 +792,14 @@ int rr_prepare_split(double t_ref, double t_absmax, const double* k, int nkc, co
   if (workspace_bytes < rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng)) return RR_ERR_WORKSPACE;
   cudaStream_t s = as_stream(stream);
   SplitTables t = carve_split(workspace, npv, npb, nlc, ng);
-  dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-  ldm_kernel<float><<<lg, 128, ldm_smem_bytes<float>(ng, nz), s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk,
-                                                                   kmin, kmax, z_edges, 0, nullptr, t.ldm);
+  if (basis && nb > 0 && nb <= MAX_BASIS && ldc) {
+    ldm_basis_kernel<float><<<npv, 128, sizeof(float) * npb * nb, s>>>(
+        law, ldc, npar, npb, k, nkc, basis, nb, nk, ng, dk, kmin, kmax, ldp, nz, z_edges, t.ldm);
+  } else {
+    dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
+    ldm_kernel<float><<<lg, 128, ldm_smem_bytes<float>(ng, nz), s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk,
+                                                                     kmin, kmax, z_edges, 0, nullptr, t.ldm);
+  }
   OrbitArgs oa{};
   oa.k = k; oa.t0 = t0; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w; oa.exptimes = exptimes;
   oa.pbids = pbids; oa.epids = epids; oa.nsamples = nsamples;
@@ -683,9 +849,22 @@ int rr_full_split(const float* times_ff, double t_ref, double t_absmax, int npt,
   if (workspace_bytes < rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng)) return RR_ERR_WORKSPACE;
   st = rr_prepare_split(t_ref, t_absmax, k, nkc, t0, ldt0, nep, p, a, inc, e, w, npv, nlc, npb, pbids, epids,
                         nsamples, exptimes, ldp, istar, weights, nk, ng, nz, dk, kmin, kmax, z_edges, workspace,
-                        workspace_bytes, stream);
+                        workspace_bytes, stream, 0, nullptr, 0, nullptr, 0);
   if (st) return st;
   return rr_flux_split(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, flux, ldflux, stream);
+}
+
+int rr_basis_count(int law, int npar) {
+  if (law < 0 || law >= LD_NLAWS) return 0;
+  return basis_count(law, npar);
+}
+
+int rr_basis_tables(int law, int npar, const double* mu, int nz, const double* W64, int nk, int ng, double* B64,
+                    float* B32, void* stream) {
+  const int nb = rr_basis_count(law, npar);
+  if (nb <= 0 || nb > MAX_BASIS || nk < 2 || ng < 2 || nz < 1 || !mu || !W64 || !B64) return RR_ERR_ARG;
+  basis_tables_kernel<<<(nk * ng + 127) / 128, 128, 0, as_stream(stream)>>>(law, nb, mu, nz, W64, nk, ng, B64, B32);
+  return check_launch("rr_basis_tables");
 }
 
 }  // extern "C"

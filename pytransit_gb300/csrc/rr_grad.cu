@@ -466,10 +466,10 @@ static int lnlike_impl(int split, int law, const double* ldc, int npar, const do
   if (split)
     st = rr_prepare_split(t_ref, t_absmax, k, nkc, t0, ldt0, nep, p, a, inc, e, w, npv, nlc, npb, pbids, epids,
                           nsamples, exptimes, (const float*)ldp, (const float*)istar, (const float*)weights, nk, ng,
-                          nz, dk, kmin, kmax, z_edges, workspace, base, stream);
+                          nz, dk, kmin, kmax, z_edges, workspace, base, stream, 0, nullptr, 0, nullptr, 0);
   else
     st = rr_prepare_f64(k, nkc, p, a, inc, e, w, npv, npb, (const double*)ldp, (const double*)weights, nk, ng, nz,
-                        dk, kmin, kmax, z_edges, workspace, base, stream);
+                        dk, kmin, kmax, z_edges, workspace, base, stream, 0, nullptr, 0, nullptr, 0);
   if (st) return st;
   const int nblk = (npt + GRAD_THREADS - 1) / GRAD_THREADS;
   Carve cv(static_cast<char*>(workspace) + base);

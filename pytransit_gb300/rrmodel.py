@@ -169,6 +169,29 @@ class RoadRunnerModel(TransitModel):
         self._tables = t
         return t
 
+    def _basis(self, device, npar, split):
+        """Basis tables of the named law (affine laws only), built once per (law, npar)."""
+        import torch
+        from . import _lib
+        if self.ld_law is None:
+            return None, 0
+        L = _lib.lib()
+        nb = L.rr_basis_count(self.ld_law, npar)
+        if nb <= 0:
+            return None, 0
+        tb = self._device_tables(device)
+        key = ('basis', npar)
+        if key not in tb:
+            nz = self.ze.size
+            B64 = torch.empty((self.nk, nb, self.ng), dtype=torch.float64, device=device)
+            B32 = torch.empty((self.nk, nb, self.ng), dtype=torch.float32, device=device)
+            _lib.check(L.rr_basis_tables(self.ld_law, npar, _lib.ptr(tb['mu']), nz, _lib.ptr(tb['W64']), self.nk,
+                                         self.ng, _lib.ptr(B64), _lib.ptr(B32), _lib.stream_ptr(device)),
+                       "rr_basis_tables")
+            tb[key] = (B64, B32)
+        B64, B32 = tb[key]
+        return (B32 if split else B64), nb
+
     def _workspace(self, nbytes, device):
         import torch
         if self._ws is None or self._ws.numel() < nbytes or self._ws.device != device:
@@ -331,34 +354,40 @@ class RoadRunnerModel(TransitModel):
         L = _lib.lib()
         stream = _lib.stream_ptr(device)
         nz = self.ze.size
+        P = _lib.ptr
+        ldc_d = args.get('ldc')
+        npar = int(ldc_d.shape[2]) if ldc_d is not None else 0
+        basis, nb = self._basis(device, npar, split) if ldc_d is not None else (None, 0)
+        kmin, kmax = float(self.klims[0]), float(self.klims[1])
         if split:
             ldf = (npt + 3) // 4 * 4
             res = torch.empty((npv, ldf), dtype=torch.float32, device=device)
             nep = t0.shape[1]
             wsb = L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, self.ng)
             ws = self._workspace(wsb, device)
-            st = L.rr_full_split(_lib.ptr(dd['times_ff']), dd['t_ref'], dd['t_absmax'], npt,
-                                 _lib.ptr(args['k']), k.shape[1], _lib.ptr(args['t0']), t0.shape[1], nep,
-                                 _lib.ptr(args['p']), _lib.ptr(args['a']), _lib.ptr(args['i']),
-                                 _lib.ptr(args['e']), _lib.ptr(args['w']), npv, nlc, npb,
-                                 _lib.ptr(dd['lcids']), _lib.ptr(dd['pbids']), _lib.ptr(dd['epids']),
-                                 _lib.ptr(dd['nsamples']), _lib.ptr(dd['exptimes']), _lib.ptr(ldp),
-                                 _lib.ptr(istar), _lib.ptr(tb['W32']), self.nk, self.ng, nz, self.dk,
-                                 float(self.klims[0]), float(self.klims[1]), self.dg, _lib.ptr(tb['ze']),
-                                 _lib.ptr(ws), ws.numel(), _lib.ptr(res), ldf, stream)
+            st = L.rr_prepare_split(dd['t_ref'], dd['t_absmax'], P(args['k']), k.shape[1], P(args['t0']),
+                                    t0.shape[1], nep, P(args['p']), P(args['a']), P(args['i']), P(args['e']),
+                                    P(args['w']), npv, nlc, npb, P(dd['pbids']), P(dd['epids']),
+                                    P(dd['nsamples']), P(dd['exptimes']), P(ldp), P(istar), P(tb['W32']), self.nk,
+                                    self.ng, nz, self.dk, kmin, kmax, P(tb['ze']), P(ws), ws.numel(), stream,
+                                    self.ld_law or 0, P(ldc_d), npar, P(basis), nb)
+            if st == 0:
+                st = L.rr_flux_split(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg,
+                                     P(ws), P(res), ldf, stream)
             res = res[:, :npt]
         else:
             res = torch.empty((npv, npt), dtype=torch.float64, device=device)
             wsb = L.rr_full_f64_workspace_bytes(npv, npb, self.ng)
             ws = self._workspace(wsb, device)
-            st = L.rr_full_f64(_lib.ptr(dd['time']), npt, _lib.ptr(args['k']), k.shape[1],
-                               _lib.ptr(args['t0']), t0.shape[1], _lib.ptr(args['p']), _lib.ptr(args['a']),
-                               _lib.ptr(args['i']), _lib.ptr(args['e']), _lib.ptr(args['w']), npv, nlc, npb,
-                               _lib.ptr(dd['lcids']), _lib.ptr(dd['pbids']), _lib.ptr(dd['epids']),
-                               _lib.ptr(dd['nsamples']), _lib.ptr(dd['exptimes']), _lib.ptr(ldp),
-                               _lib.ptr(istar), _lib.ptr(tb['W64']), self.nk, self.ng, nz, self.dk,
-                               float(self.klims[0]), float(self.klims[1]), self.dg, _lib.ptr(tb['ze']),
-                               _lib.ptr(ws), ws.numel(), _lib.ptr(res), npt, stream)
+            st = L.rr_prepare_f64(P(args['k']), k.shape[1], P(args['p']), P(args['a']), P(args['i']),
+                                  P(args['e']), P(args['w']), npv, npb, P(ldp), P(tb['W64']), self.nk, self.ng, nz,
+                                  self.dk, kmin, kmax, P(tb['ze']), P(ws), ws.numel(), stream,
+                                  self.ld_law or 0, P(ldc_d), npar, P(basis), nb)
+            if st == 0:
+                st = L.rr_flux_f64(P(dd['time']), npt, P(args['k']), k.shape[1], P(args['t0']), t0.shape[1],
+                                   P(args['p']), npv, nlc, npb, P(dd['lcids']), P(dd['pbids']), P(dd['epids']),
+                                   P(dd['nsamples']), P(dd['exptimes']), P(istar), self.ng, self.dg, P(ws),
+                                   P(res), npt, stream)
         _lib.check(st, "rr_full")
         if user_out is not None:
             src = res if user_out.dtype == res.dtype else res.to(user_out.dtype)
