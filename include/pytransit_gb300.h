@@ -159,6 +159,29 @@ int rr_prepare_split(double t_ref, double t_absmax, const double *k, int nkc, co
 int rr_flux_split(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb, int ng,
                   double dg, const void *workspace, float *flux, int ldflux, void *stream);
 
+/* ---- transmission-spectroscopy model --------------------------------------- */
+
+/* Replaces tsmodel_serial (pytransit/models/roadrunner/model_trspec.py:12-93)
+ * behind TransmissionSpectroscopyModel.evaluate (tsmodel.py:46-130): k[npv, npb]
+ * one radius ratio per channel, t0[npv], ldp[npv, npb, nz], istar[npv, npb];
+ * weights = NULL uses the 2D table at the mean radius ratio (the reference's
+ * default), a 3D table the reference's precompute_weights rule.  Only
+ * nsamples0 and exptime0 (the first light curve's) are used, as in the
+ * reference.  -> flux[npv, npb, ldflux]. */
+size_t rr_ts_workspace_bytes(int split, int npv, int npb, int ng);
+int rr_ts_f64(const double *times, int npt, const double *k, const double *t0, const double *p,
+              const double *a, const double *inc, const double *e, const double *w, int npv, int npb,
+              int nsamples0, double exptime0, const double *ldp, const double *istar, const double *weights,
+              int nk, int ng, int nz, double dk, double kmin, double kmax, double dg, const double *z_edges,
+              void *workspace, size_t workspace_bytes, double *flux, int ldflux, void *stream);
+/* Same, split precision (times_ff and t_ref/t_absmax as rr_full_split). */
+int rr_ts_split(const float *times_ff, double t_ref, double t_absmax, int npt, const double *k,
+                const double *t0, const double *p, const double *a, const double *inc, const double *e,
+                const double *w, int npv, int npb, int nsamples0, double exptime0, const float *ldp,
+                const float *istar, const float *weights, int nk, int ng, int nz, double dk, double kmin,
+                double kmax, double dg, const double *z_edges, void *workspace, size_t workspace_bytes,
+                float *flux, int ldflux, void *stream);
+
 /* ---- Gaussian log-likelihood and its gradient ----------------------------- */
 
 /* Fused model + Gaussian log-likelihood per parameter vector

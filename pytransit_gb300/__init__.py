@@ -8,8 +8,10 @@ pytransit/models/__init__.py:17-26).
 from .transitmodel import TransitModel
 from .ldmodel import LDModel
 from .rrmodel import RoadRunnerModel, create_z_grid
+from .tsmodel import TransmissionSpectroscopyModel, TSModel
 
 RRModel = RoadRunnerModel
 
-__all__ = ['TransitModel', 'LDModel', 'RoadRunnerModel', 'RRModel', 'create_z_grid']
+__all__ = ['TransitModel', 'LDModel', 'RoadRunnerModel', 'RRModel', 'TransmissionSpectroscopyModel', 'TSModel',
+           'create_z_grid']
 __version__ = '0.1.0'

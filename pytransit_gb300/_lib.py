@@ -53,6 +53,12 @@ def _sig(L):
                                     _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _vp, _vp, _sz, _vp,
                                     _i, _vp, _i, _vp, _i])
     L.rr_flux_split.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _vp, _i, _vp]
+    L.rr_ts_workspace_bytes.argtypes = [_i, _i, _i, _i]
+    L.rr_ts_workspace_bytes.restype = _sz
+    _ts_tail = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _d,
+                _vp, _vp, _sz, _vp, _i, _vp]
+    L.rr_ts_f64.argtypes = [_vp, _i] + _ts_tail
+    L.rr_ts_split.argtypes = [_vp, _d, _d, _i] + _ts_tail
     for name, args in _EXTRA_SIGNATURES.items():
         if hasattr(L, name):
             getattr(L, name).argtypes = args[0]

@@ -94,6 +94,26 @@ static size_t ldm_smem_bytes(int ng, int nz) {
   return sizeof(R) * ((size_t)ng * (nz + 1) + (size_t)LDM_PBB * nz);
 }
 
+// Host launchers of the LD-means kernel for the other translation units.
+template <typename R>
+static void launch_ldm_impl(const R* ldp, int npv, int npb, int nz, const double* kw, int kw_stride, const R* W,
+                            int nk, int ng, double dk, double kmin, double kmax, const double* ze, int mode,
+                            const double* kmax_pv, R* ldm, cudaStream_t s) {
+  dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
+  ldm_kernel<R><<<lg, 128, ldm_smem_bytes<R>(ng, nz), s>>>(ldp, npb, nz, kw, kw_stride, W, nk, ng, dk, kmin, kmax,
+                                                          ze, mode, kmax_pv, ldm);
+}
+void launch_ldm_f32(const float* ldp, int npv, int npb, int nz, const double* kw, int kw_stride, const float* W,
+                    int nk, int ng, double dk, double kmin, double kmax, const double* ze, int mode,
+                    const double* kmax_pv, float* ldm, cudaStream_t s) {
+  launch_ldm_impl<float>(ldp, npv, npb, nz, kw, kw_stride, W, nk, ng, dk, kmin, kmax, ze, mode, kmax_pv, ldm, s);
+}
+void launch_ldm_f64(const double* ldp, int npv, int npb, int nz, const double* kw, int kw_stride, const double* W,
+                    int nk, int ng, double dk, double kmin, double kmax, const double* ze, int mode,
+                    const double* kmax_pv, double* ldm, cudaStream_t s) {
+  launch_ldm_impl<double>(ldp, npv, npb, nz, kw, kw_stride, W, nk, ng, dk, kmin, kmax, ze, mode, kmax_pv, ldm, s);
+}
+
 // ---------------------------------------------------------------------------
 // Basis tables of an affine law: B[ik][b][g] = sum_z W[ik][g][z] phi_b(mu_z),
 // one thread per (ik, g), FP64 (and an FP32 copy).

@@ -12,6 +12,15 @@ namespace rr {
 int check_launch(const char* where);
 void set_cuda_error(cudaError_t e, const char* where);
 
+// LD-means kernel launchers (rr_full.cu); mode 0: rr_full rule, 1: the
+// transmission-spectroscopy rule with kmax_pv, 2: always the 2D table.
+void launch_ldm_f32(const float* ldp, int npv, int npb, int nz, const double* kw, int kw_stride, const float* W,
+                    int nk, int ng, double dk, double kmin, double kmax, const double* ze, int mode,
+                    const double* kmax_pv, float* ldm, cudaStream_t s);
+void launch_ldm_f64(const double* ldp, int npv, int npb, int nz, const double* kw, int kw_stride, const double* W,
+                    int nk, int ng, double dk, double kmin, double kmax, const double* ze, int mode,
+                    const double* kmax_pv, double* ldm, cudaStream_t s);
+
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // Bump allocator over a caller-owned workspace (256-byte aligned pieces).

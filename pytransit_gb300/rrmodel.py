@@ -294,8 +294,8 @@ class RoadRunnerModel(TransitModel):
         except ValueError:
             raise ValueError(f"The limb darkening model returned ldp {ldp.shape} and istar {istar.shape}; "
                              f"expected [{npv}, {npb}, {nz}] and [{npv}, {npb}].") from None
-        ldp_d = torch.as_tensor(np.ascontiguousarray(ldp)).to(device=device, dtype=dt)
-        istar_d = torch.as_tensor(np.ascontiguousarray(istar)).to(device=device, dtype=dt)
+        ldp_d = torch.as_tensor(np.array(ldp, dtype=np.float64)).to(device=device, dtype=dt)
+        istar_d = torch.as_tensor(np.array(istar, dtype=np.float64)).to(device=device, dtype=dt)
         return ldp_d, istar_d
 
     def _upload(self, arrays, device):

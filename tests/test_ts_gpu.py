@@ -1,0 +1,78 @@
+"""Transmission-spectroscopy model on the GPU vs the reference's own code
+(golden fixture) and the oracle's restatement of tsmodel_serial.
+
+Tolerances: FP64 path 1e-9, split path 1e-6 (max |dF|); NaN rows match."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = {'fp64': 1e-9, 'split': 1e-6}
+
+
+def ts(precision, interp=False, law='quadratic'):
+    from pytransit_gb300 import TransmissionSpectroscopyModel
+    return TransmissionSpectroscopyModel(law, precision=precision, precompute_weights=interp)
+
+
+def max_err(got, want):
+    assert got.shape == want.shape
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    m = ~np.isnan(want)
+    return float(np.abs(got[m] - want[m]).max()) if m.any() else 0.0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("variant", ["2d", "3d"])
+def test_ts_golden(golden, precision, variant):
+    g = golden("ts")
+    m = ts(precision, interp=(variant == "3d"))
+    m.set_data(g["time"], nsamples=[3], exptimes=[0.01])
+    flux = m.evaluate(g["k"], g["ldc"], g["t0"], g["p"], g["a"], g["inc"], g["e"], g["w"])
+    assert max_err(flux, g[f"flux__{variant}"]) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_ts_200_channels_vs_oracle(precision):
+    """200 channels, k ~ U(0.09, 0.11), 10 supersamples, BJD-scale times,
+    eccentric orbits, plus an invalid parameter vector (NaN row)."""
+    rng = np.random.default_rng(31)
+    T = 2459000.0
+    time = T + np.linspace(-0.25, 0.25, 900)
+    npv, npb = 6, 200
+    k = rng.uniform(0.09, 0.11, (npv, npb))
+    ldc = np.stack([rng.uniform(0.2, 0.5, (npv, npb)), rng.uniform(0.1, 0.3, (npv, npb))], -1)
+    t0 = T + rng.normal(0, 1e-3, npv)
+    p = rng.uniform(1, 5, npv)
+    a = rng.uniform(4, 12, npv)
+    inc = np.arccos(rng.uniform(0, 0.8, npv) / a)
+    e = rng.uniform(0, 0.2, npv)
+    w = rng.uniform(0, 2 * np.pi, npv)
+    a[3] = 0.5
+    ref = oracle.OracleRoadRunner('quadratic', ts=True)
+    ref.set_data(time, nsamples=[10], exptimes=[1 / 48])
+    want = ref.evaluate(k, ldc, t0, p, a, inc, e, w)
+    m = ts(precision)
+    m.set_data(time, nsamples=[10], exptimes=[1 / 48])
+    got = m.evaluate(k, ldc, t0, p, a, inc, e, w)
+    assert np.isnan(got[3]).all()
+    assert np.sum(want[~np.isnan(want)] < 1) > 10000
+    assert max_err(got, want) <= TOL[precision]
+
+
+def test_ts_many_samples_chunked():
+    """More than 32 supersamples: the sample loop runs in chunks of 32."""
+    rng = np.random.default_rng(2)
+    time = np.linspace(-0.15, 0.15, 300)
+    npv, npb = 3, 40
+    k = rng.uniform(0.09, 0.11, (npv, npb))
+    ldc = np.tile([0.4, 0.2], (npv, npb, 1))
+    args = (k, ldc, np.zeros(npv), np.full(npv, 2.5), np.full(npv, 7.0), np.full(npv, np.arccos(0.3 / 7)),
+            np.zeros(npv), np.zeros(npv))
+    ref = oracle.OracleRoadRunner('quadratic', ts=True)
+    ref.set_data(time, nsamples=[45], exptimes=[0.03])
+    m = ts('fp64')
+    m.set_data(time, nsamples=[45], exptimes=[0.03])
+    assert max_err(m.evaluate(*args), ref.evaluate(*args)) <= 1e-9
