@@ -217,6 +217,39 @@ int rr_lnlike_split(int law, const double *ldc, int npar, const double *mu, cons
                     double kmax, double dg, const double *z_edges, const double *obs, const double *sigma,
                     void *workspace, size_t workspace_bytes, double *lnl, double *grad, void *stream);
 
+/* ---- serving: many requests in one persistent launch ---------------------- */
+
+/* One request of the serving loop (all pointers on the device): the data of
+ * rr_time_split (times_ff) and set_data (lcids), the tables written by
+ * rr_prepare_split (rr_full_split_tables gives their addresses inside the
+ * workspace) and the request's output flux[npv, ldflux]. */
+typedef struct {
+  const float *times_ff;
+  const int32_t *lcids;
+  const float *orb32;
+  const float *lc32;
+  const float *ldm;
+  float *flux;
+  int64_t ldflux;
+  int32_t npt, npv, nlc, npb, ng, pad0;
+  float inv_dg, pad1;
+} rr_serve_request;
+
+/* A unit of work: parameter vectors [pv0, pv1) x 128-point tiles [tile0, tile1) of request req. */
+typedef struct {
+  int32_t req, pv0, pv1, tile0, tile1, pad;
+} rr_serve_item;
+
+/* sizeof(rr_serve_request), sizeof(rr_serve_item) (for bindings that build the arrays) */
+void rr_serve_struct_sizes(int *request_size, int *item_size);
+void rr_full_split_tables(void *workspace, int npv, int npb, int nlc, int nep, int ng, const float **orb32,
+                          const float **lc32, const float **ldm);
+/* No counterpart in the reference (serving layer): nblocks persistent blocks
+ * take the items items[0 .. *nitems) from *counter (set to 0 beforehand) and
+ * write every covered flux value of the requests; returns at launch. */
+int rr_serve_flux_split(const rr_serve_request *reqs, const rr_serve_item *items, const int *nitems, int *counter,
+                        int nblocks, void *stream);
+
 /* ---- no-allocation variant ------------------------------------------------- */
 
 /* No counterpart in the reference: an addition for callers that cannot

@@ -99,6 +99,8 @@ def require_cuda(device=None) -> torch.device:
     dev = torch.device(device if device is not None else "cuda")
     if dev.type != "cuda":
         raise RuntimeError(f"pytransit_gb300 runs on CUDA devices only, not {dev}")
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
     return dev
 
 

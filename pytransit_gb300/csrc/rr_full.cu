@@ -594,26 +594,23 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
   __syncwarp();
 }
 
-// Grid: x = ranges of warp tiles, y/z = parameter vectors.  The block stages
-// its pv's orbit and light-curve records in shared memory; each warp loops
-// over tiles.  A tile whose time range (from the precomputed tile summary)
-// misses every box copy of its light curve is written as 1.0 straight away;
-// other tiles load their times and take the per-point path.
-template <bool LC_IN_SMEM>
-__global__ void __launch_bounds__(SPLIT_WARPS * 32) flux_split_kernel(FluxSplitArgs A) {
-  __shared__ WarpList lists[SPLIT_WARPS];
-  __shared__ __align__(16) float recs[ORB32 + (LC_IN_SMEM ? LC_SMEM * LC32 : 0)];
-  const unsigned FULL = 0xffffffffu;
+// One block's share of one parameter vector: stage the pv's orbit and
+// light-curve records in shared memory, then the warps loop over the tiles
+// t_first + warp, + t_step, ... below t_end.  A tile whose time range (from
+// the precomputed tile summary) misses every box copy of its light curve is
+// written as 1.0 straight away; other tiles load their times and take the
+// per-point path.  Ends without a barrier: the caller synchronises before
+// staging another pv.
+__device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, int t_first, int t_step, int t_end,
+                                               float* recs, bool lc_in_smem, WarpList* lists) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int pv = block_pv();
-  if (pv >= A.npv) return;  // block-uniform
   const float* lcg = A.lc32 + (size_t)pv * A.nlc * LC32;
   if (threadIdx.x < ORB32) recs[threadIdx.x] = __ldg(A.orb32 + (size_t)pv * ORB32 + threadIdx.x);
-  if (LC_IN_SMEM)
+  if (lc_in_smem)
     for (int i = threadIdx.x; i < A.nlc * LC32; i += blockDim.x) recs[ORB32 + i] = __ldg(lcg + i);
   __syncthreads();
   const float* orb = recs;
-  const float* LCR = LC_IN_SMEM ? recs + ORB32 : lcg;
+  const float* LCR = lc_in_smem ? recs + ORB32 : lcg;
   const int flags = __float_as_int(orb[14]);
   const bool valid = flags & FLAG_VALID;
   const bool wide = flags & FLAG_WIDE;
@@ -624,8 +621,7 @@ __global__ void __launch_bounds__(SPLIT_WARPS * 32) flux_split_kernel(FluxSplitA
   const float4* meta = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(A.times_ff) +
                                                        time_meta_offset(A.npt));
   WarpList& L = lists[warp];
-  const int ntiles = (A.npt + WARP_TILE - 1) / WARP_TILE;
-  for (int tile = blockIdx.x * SPLIT_WARPS + warp; tile < ntiles; tile += gridDim.x * SPLIT_WARPS) {
+  for (int tile = t_first + warp; tile < t_end; tile += t_step) {
     const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
     const bool full4 = pt0 + SPLIT_PTS <= A.npt;
     float res[SPLIT_PTS] = {1.0f, 1.0f, 1.0f, 1.0f};
@@ -682,6 +678,52 @@ __global__ void __launch_bounds__(SPLIT_WARPS * 32) flux_split_kernel(FluxSplitA
     } else {
       for (int q = 0; q < SPLIT_PTS; ++q)
         if (pt0 + q < A.npt) __stcs(row + pt0 + q, res[q]);
+    }
+  }
+}
+
+// Grid: x = ranges of warp tiles, y/z = parameter vectors.
+template <bool LC_IN_SMEM>
+__global__ void __launch_bounds__(SPLIT_WARPS * 32) flux_split_kernel(FluxSplitArgs A) {
+  __shared__ WarpList lists[SPLIT_WARPS];
+  __shared__ __align__(16) float recs[ORB32 + (LC_IN_SMEM ? LC_SMEM * LC32 : 0)];
+  const int pv = block_pv();
+  if (pv >= A.npv) return;  // block-uniform
+  const int ntiles = (A.npt + WARP_TILE - 1) / WARP_TILE;
+  split_pv_tiles(A, pv, blockIdx.x * SPLIT_WARPS, gridDim.x * SPLIT_WARPS, ntiles, recs, LC_IN_SMEM, lists);
+}
+
+// ---------------------------------------------------------------------------
+// Serving: one persistent launch over the work items of many requests.  Each
+// block takes the next item (request, pv range, tile range) from a device
+// counter and runs split_pv_tiles for it with that request's tables; the
+// item list is complete at launch, so no block ever waits for work.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPLIT_WARPS * 32)
+serve_split_kernel(const rr_serve_request* __restrict__ reqs, const rr_serve_item* __restrict__ items,
+                   const int* __restrict__ nitems_p, int* __restrict__ counter) {
+  __shared__ WarpList lists[SPLIT_WARPS];
+  __shared__ __align__(16) float recs[ORB32 + LC_SMEM * LC32];
+  __shared__ int s_item;
+  const int nitems = *nitems_p;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    if (it >= nitems) return;
+    const rr_serve_item w = items[it];
+    const rr_serve_request& r = reqs[w.req];
+    FluxSplitArgs A{};
+    A.times_ff = reinterpret_cast<const float2*>(r.times_ff);
+    A.lcids = r.lcids;
+    A.orb32 = r.orb32; A.lc32 = r.lc32; A.ldm = r.ldm;
+    A.npt = r.npt; A.npv = r.npv; A.npb = r.npb; A.nlc = r.nlc; A.ng = r.ng; A.ldflux = (int)r.ldflux;
+    A.inv_dg = r.inv_dg; A.flux = r.flux;
+    const bool lc_smem = r.nlc <= LC_SMEM;
+    for (int pv = w.pv0; pv < w.pv1; ++pv) {
+      split_pv_tiles(A, pv, w.tile0, SPLIT_WARPS, w.tile1, recs, lc_smem, lists);
+      __syncthreads();
     }
   }
 }
@@ -872,6 +914,27 @@ int rr_full_split(const float* times_ff, double t_ref, double t_absmax, int npt,
                         workspace_bytes, stream, 0, nullptr, 0, nullptr, 0);
   if (st) return st;
   return rr_flux_split(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, flux, ldflux, stream);
+}
+
+void rr_full_split_tables(void* workspace, int npv, int npb, int nlc, int nep, int ng, const float** orb32,
+                          const float** lc32, const float** ldm) {
+  (void)nep;
+  SplitTables t = carve_split(workspace, npv, npb, nlc, ng);
+  if (orb32) *orb32 = t.orb;
+  if (lc32) *lc32 = t.lc;
+  if (ldm) *ldm = t.ldm;
+}
+
+void rr_serve_struct_sizes(int* request_size, int* item_size) {
+  if (request_size) *request_size = (int)sizeof(rr_serve_request);
+  if (item_size) *item_size = (int)sizeof(rr_serve_item);
+}
+
+int rr_serve_flux_split(const rr_serve_request* reqs, const rr_serve_item* items, const int* nitems, int* counter,
+                        int nblocks, void* stream) {
+  if (!reqs || !items || !nitems || !counter || nblocks < 1) return RR_ERR_ARG;
+  serve_split_kernel<<<nblocks, SPLIT_WARPS * 32, 0, as_stream(stream)>>>(reqs, items, nitems, counter);
+  return check_launch("rr_serve_flux_split");
 }
 
 int rr_basis_count(int law, int npar) {

@@ -133,3 +133,17 @@ def test_no_cpu_fallback():
     m.set_data(np.linspace(-0.1, 0.1, 10))
     with pytest.raises(RuntimeError, match="CUDA"):
         m.evaluate(0.1, [0.3, 0.1], 0.0, 2.0, 7.0, 1.55)
+
+
+def test_serving_struct_layout_matches_binding():
+    import ctypes as C
+    import numpy as np
+    from pytransit_gb300 import _lib
+    L = _lib.lib()
+    L.rr_serve_struct_sizes.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    rs, its = C.c_int(), C.c_int()
+    L.rr_serve_struct_sizes(C.byref(rs), C.byref(its))
+    dt = np.dtype([('times_ff', 'u8'), ('lcids', 'u8'), ('orb32', 'u8'), ('lc32', 'u8'), ('ldm', 'u8'),
+                   ('flux', 'u8'), ('ldflux', 'i8'), ('npt', 'i4'), ('npv', 'i4'), ('nlc', 'i4'), ('npb', 'i4'),
+                   ('ng', 'i4'), ('pad0', 'i4'), ('inv_dg', 'f4'), ('pad1', 'f4')])
+    assert rs.value == dt.itemsize and its.value == 24
