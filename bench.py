@@ -202,6 +202,221 @@ def impl_reference(args, rank):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Other workloads: precision form (C2), differentiation (C3), serving (C4)
+# ---------------------------------------------------------------------------
+
+def c2_workload(npv=4096, seed=2024):
+    """16 light curves, npt log-uniform in [500, 50000] at 30-min cadence from BJD
+    2459000, nsamples = 10 with 30-min exposures, passbands j mod 4; power-2 LD;
+    eccentric orbits; other parameters as the default workload."""
+    rng = np.random.default_rng(seed)
+    T = 2459000.0
+    npts = np.exp(rng.uniform(np.log(500), np.log(50000), 16)).astype(int)
+    time_ = np.concatenate([T + np.arange(n) / 48.0 for n in npts])
+    lcids = np.concatenate([np.full(n, j) for j, n in enumerate(npts)])
+    data = dict(time=time_, lcids=lcids, pbids=np.arange(16) % 4, nsamples=np.full(16, 10),
+                exptimes=np.full(16, 1 / 48))
+    a = rng.uniform(3.0, 20.0, npv)
+    prm = dict(k=rng.uniform(0.05, 0.15, (npv, 1)),
+               ldc=np.stack([rng.uniform(.3, .9, (npv, 4)), rng.uniform(.3, .8, (npv, 4))], -1),
+               t0=T + rng.normal(0, 1e-3, (npv, 1)), p=rng.uniform(0.5, 15.0, npv), a=a,
+               i=np.arccos(rng.uniform(0.0, 0.9, npv) / a), e=rng.uniform(0, 0.3, npv),
+               w=rng.uniform(0, 2 * np.pi, npv))
+    return data, prm
+
+
+def bench_model(model, prm, steps, torch, device):
+    """Mean ms of model.evaluate(copy=False) (parameters uploaded each call)."""
+    args = (prm["k"], prm["ldc"], prm["t0"], prm["p"], prm["a"], prm["i"], prm["e"], prm["w"])
+    out = model.evaluate(*args, copy=False)
+    torch.cuda.synchronize(device)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(steps):
+        out = model.evaluate(*args, copy=False)
+    t1.record()
+    torch.cuda.synchronize(device)
+    return t0.elapsed_time(t1) / steps, out
+
+
+def bench_c2(torch, device, steps=5):
+    from pytransit_gb300 import RoadRunnerModel
+    data, prm = c2_workload()
+    npv, npt = prm["p"].size, data["time"].size
+    res = {}
+    for prec in ("split", "fp64"):
+        m = RoadRunnerModel('power-2', precision=prec, device=device)
+        m.set_data(**data)
+        ms, out = bench_model(m, prm, steps if prec == "split" else 2, torch, device)
+        res[prec] = (ms, out)
+    dF = float((res["split"][1].double() - res["fp64"][1]).abs().max().item())
+    pts = npv * npt
+    return {"workload": f"{npv} pv x {npt} times (16 light curves, 30-min cadence, 10 supersamples, 4 passbands, "
+                        "power-2 LD, eccentric)",
+            "split_points_per_s": pts / (res["split"][0] / 1e3), "fp64_points_per_s": pts / (res["fp64"][0] / 1e3),
+            "split_ms": res["split"][0], "fp64_ms": res["fp64"][0],
+            "split_over_fp64": res["fp64"][0] / res["split"][0], "max_abs_dF_vs_fp64": dF,
+            "timed": "RoadRunnerModel.evaluate(copy=False), CUDA events, parameters uploaded each call"}
+
+
+def bench_c3(torch, device, steps=3):
+    """Log-likelihood + adjoint gradient, 4096 pv x 5000 times, 5 supersamples."""
+    from pytransit_gb300 import RoadRunnerModel
+    from pytransit_gb300.lnlike import lnlikelihood
+    rng = np.random.default_rng(77)
+    npv, npt, sigma = 4096, 5000, 5e-4
+    data = dict(time=np.linspace(-0.2, 0.2, npt), nsamples=[5], exptimes=[1 / 48])
+    a0 = rng.uniform(3, 20)
+    truth = dict(k=np.array([[rng.uniform(.05, .15)]]), ldc=np.array([[[rng.uniform(0, .6), rng.uniform(0, .3)]]]),
+                 t0=np.array([[rng.normal(0, 1e-3)]]), p=np.array([rng.uniform(1, 10)]), a=np.array([a0]),
+                 i=np.array([np.arccos(rng.uniform(0, .9) / a0)]), e=np.array([rng.uniform(0, .3)]),
+                 w=np.array([rng.uniform(0, 2 * np.pi)]))
+    m64 = RoadRunnerModel('quadratic', precision='fp64', device=device)
+    m64.set_data(**data)
+    f_true = m64.evaluate(truth["k"], truth["ldc"], truth["t0"], truth["p"], truth["a"], truth["i"], truth["e"],
+                          truth["w"])
+    obs = f_true + rng.normal(0, sigma, npt)
+    prm = dict(k=truth["k"] * (1 + rng.normal(0, 0.02, (npv, 1))),
+               ldc=np.clip(truth["ldc"] + rng.normal(0, 0.02, (npv, 1, 2)), 0.01, None),
+               t0=truth["t0"] + rng.normal(0, 2e-4, (npv, 1)), p=truth["p"] * (1 + rng.normal(0, 1e-4, npv)),
+               a=truth["a"] * (1 + rng.normal(0, 0.01, npv)), i=truth["i"] + rng.normal(0, 1e-3, npv),
+               e=np.clip(truth["e"] + rng.normal(0, 0.01, npv), 0, None), w=truth["w"] + rng.normal(0, 0.05, npv))
+    out = {}
+    for prec in ("split", "fp64"):
+        m = RoadRunnerModel('quadratic', precision=prec, device=device)
+        m.set_data(**data)
+        args = (m, obs, sigma, prm["k"], prm["ldc"], prm["t0"], prm["p"], prm["a"], prm["i"], prm["e"], prm["w"])
+        lnlikelihood(*args, grad=True, copy=False)
+        torch.cuda.synchronize(device)
+        t = time.perf_counter()
+        n = steps if prec == "split" else 1
+        for _ in range(n):
+            lnl, g = lnlikelihood(*args, grad=True, copy=False)
+        torch.cuda.synchronize(device)
+        out[prec] = ((time.perf_counter() - t) / n, lnl.cpu().numpy(), g.cpu().numpy())
+    g32, g64 = out["split"][2], out["fp64"][2]
+    col_rel = float((np.abs(g32 - g64) / np.abs(g64).max(axis=0, keepdims=True)).max())
+    lnl_rel = float(np.abs(out["split"][1] - out["fp64"][1]).max() / np.abs(out["fp64"][1]).max())
+    return {"workload": f"{npv} pv x {npt} times, 5 supersamples, quadratic LD, Gaussian lnL sigma=5e-4, "
+                        "gradient wrt (k, t0, p, a, i, e, w, u1, u2)",
+            "split_ms": out["split"][0] * 1e3, "fp64_ms": out["fp64"][0] * 1e3,
+            "split_points_per_s": npv * npt / out["split"][0], "fp64_points_per_s": npv * npt / out["fp64"][0],
+            "split_over_fp64": out["fp64"][0] / out["split"][0],
+            "grad_max_rel_err_split_vs_fp64": col_rel, "lnl_max_rel_err_split_vs_fp64": lnl_rel,
+            "timed": "lnlikelihood(grad=True) end to end (LD tables, prologue, fused lnL + adjoint), wall clock"}
+
+
+def c4_requests(nreq, seed=4):
+    """The serving mix: npv log-uniform [1, 4096], npt log-uniform [500, 1e5],
+    nsamples in {1, 5, 10}, LD in {quadratic, power-2, nonlinear}, 20 %
+    transmission-spectroscopy requests with 200 channels, k ~ U(0.09, 0.11)."""
+    rng = np.random.default_rng(seed)
+    T = 2459000.0
+    out = []
+    for j in range(nreq):
+        kind = 'ts' if rng.uniform() < 0.2 else 'rr'
+        law = ['quadratic', 'power-2', 'nonlinear'][int(rng.integers(0, 3))]
+        npv = int(np.exp(rng.uniform(0, np.log(4096))))
+        npt = int(np.exp(rng.uniform(np.log(500), np.log(1e5))))
+        ns = int(rng.choice([1, 5, 10]))
+        cad = 2 / 1440
+        time_ = T + np.arange(npt) * cad
+        npb = 200 if kind == 'ts' else 1
+        if law == 'nonlinear':
+            ldc = np.tile([0.5, -0.2, 0.6, -0.25], (npv, npb, 1))
+        elif law == 'power-2':
+            ldc = np.tile([0.6, 0.55], (npv, npb, 1))
+        else:
+            ldc = np.tile([0.35, 0.15], (npv, npb, 1))
+        k = rng.uniform(0.09, 0.11, (npv, npb)) if kind == 'ts' else rng.uniform(0.05, 0.15, (npv, 1))
+        a = rng.uniform(3, 20, npv)
+        params = dict(k=k, ldc=ldc, t0=T + rng.normal(0, 1e-3, npv), p=rng.uniform(0.5, 15, npv), a=a,
+                      i=np.arccos(rng.uniform(0, 0.9, npv) / a), e=np.zeros(npv), w=np.zeros(npv))
+        data = dict(time=time_, nsamples=[ns], exptimes=[cad if ns > 1 else 0.0])
+        out.append((kind, law, data, params))
+    return out
+
+
+def bench_serve(args):
+    """Poisson stream at --rate requests/s through RRServer (device-resident
+    results); p50/p99 latency, throughput; the plain FP64 path run per request
+    on the first requests for comparison."""
+    import threading
+    import torch
+    from pytransit_gb300 import RoadRunnerModel, TransmissionSpectroscopyModel
+    from pytransit_gb300.serving import RRServer
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    reqs = c4_requests(args.nreq)
+    rng = np.random.default_rng(5)
+    gaps = rng.exponential(1.0 / args.rate, len(reqs))
+    srv = RRServer(hbm_budget=120e9, result='device', device=device)
+    # warm-up (tables, graph, allocator)
+    srv.submit(*c4_requests(2, seed=99)[0], keep_result=False).result()
+    done_t = {}
+    futs = []
+    t_start = time.perf_counter()
+    t_next = t_start
+    for j, (r, gap) in enumerate(zip(reqs, gaps)):
+        t_next += gap
+        while time.perf_counter() < t_next:
+            time.sleep(0.0001)
+        f = srv.submit(*r, keep_result=False)
+        f.add_done_callback(lambda fut, j=j: done_t.__setitem__(j, time.perf_counter()))
+        futs.append(f)
+    ok = 0
+    points = 0
+    for j, f in enumerate(futs):
+        try:
+            points += f.result()
+            ok += 1
+        except MemoryError:
+            pass
+        futs[j] = None
+    t_end = time.perf_counter()
+    stats = srv.stats.summary()
+    srv.close()
+    # plain FP64 path, one request at a time (bounded sample)
+    n_plain, t_plain, pts_plain = 0, 0.0, 0
+    for kind, law, data, params in reqs[:args.plain_sample]:
+        M = TransmissionSpectroscopyModel if kind == 'ts' else RoadRunnerModel
+        m = M(law, precision='fp64', device=device)
+        if kind == 'ts':
+            m.set_data(data["time"], nsamples=data["nsamples"], exptimes=data["exptimes"])
+            argv = (params["k"], params["ldc"], params["t0"], params["p"], params["a"], params["i"], params["e"],
+                    params["w"])
+        else:
+            m.set_data(**data)
+            argv = (params["k"], params["ldc"], params["t0"].reshape(-1, 1), params["p"], params["a"], params["i"],
+                    params["e"], params["w"])
+        torch.cuda.synchronize(device)
+        t = time.perf_counter()
+        out = m.evaluate(*argv, copy=False)
+        torch.cuda.synchronize(device)
+        t_plain += time.perf_counter() - t
+        pts_plain += out.numel()
+        n_plain += 1
+        del out, m
+    line = {"metric": "served model points/s (Poisson request stream); p50/p99 latency",
+            "value": points / (t_end - t_start), "unit": "model points/s", "n_gpus": 1,
+            "higher_is_better": True, "data": "synthetic (seeded)",
+            "config": {"workload": f"{len(reqs)} requests, Poisson arrivals at {args.rate} req/s; npv log-U[1,4096], "
+                                   "npt log-U[500,1e5], nsamples {1,5,10}, LD {quadratic, power-2, nonlinear}, 20% TS "
+                                   "with 200 channels; split precision; results kept on the device; HBM budget 120 GB"},
+            "latency_p50_s": stats["p50_s"], "latency_p99_s": stats["p99_s"], "latency_mean_s": stats["mean_s"],
+            "completed": stats["completed"], "rejected": stats["rejected"], "steps": stats["steps"],
+            "wall_s": t_end - t_start, "offered_req_per_s": args.rate,
+            "achieved_req_per_s": stats["completed"] / (t_end - t_start),
+            "peak_admitted_bytes": stats["peak_hbm_bytes"],
+            "plain_fp64_per_request": {"requests": n_plain, "points_per_s": pts_plain / max(t_plain, 1e-9),
+                                       "sample": f"first {n_plain} requests, one at a time, RoadRunnerModel / "
+                                                 "TransmissionSpectroscopyModel precision='fp64', copy=False"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -211,6 +426,11 @@ def main():
     ap.add_argument("--npv", type=int, default=8192)
     ap.add_argument("--npt", type=int, default=19700)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the precision and gradient workloads")
+    ap.add_argument("--workload", default="c1", choices=["c1", "serve"])
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--nreq", type=int, default=300)
+    ap.add_argument("--plain-sample", type=int, default=20)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -220,6 +440,8 @@ def main():
 
     if args.impl == "reference":
         return impl_reference(args, rank)
+    if args.workload == "serve":
+        return bench_serve(args) if rank == 0 else 0
 
     import torch
     import torch.distributed as dist
@@ -389,6 +611,9 @@ def main():
         "clocks": clocks,
         "gpu_launches": 4 * args.steps,
     }
+    if rank == 0 and not args.no_extra:
+        line["c2_precision"] = bench_c2(torch, device)
+        line["c3_gradient"] = bench_c3(torch, device)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_baseline(data, prm)
     if rank == 0:

@@ -143,8 +143,8 @@ class RRServer:
     """Continuous-batching server (see the module docstring)."""
 
     def __init__(self, executor=None, hbm_budget: float = 120e9, step_items: int = 4096,
-                 ts_chunk_bytes: float = 4e9, device=None):
-        self.ex = executor if executor is not None else GpuExecutor(device)
+                 ts_chunk_bytes: float = 4e9, device=None, result: str = 'host'):
+        self.ex = executor if executor is not None else GpuExecutor(device, result=result)
         self.budget = int(hbm_budget)
         self.step_items = step_items
         self.ts_chunk_bytes = ts_chunk_bytes
@@ -159,12 +159,18 @@ class RRServer:
         self._thread.start()
 
     # -- client side ------------------------------------------------------
-    def submit(self, kind: str, ld: str, data: dict, params: dict) -> cf.Future:
+    def submit(self, kind: str, ld: str, data: dict, params: dict, keep_result: bool = True) -> cf.Future:
+        """Queue one evaluation.  The future resolves to the flux (numpy in
+        pinned host memory, or a CUDA tensor with result='device'); with
+        keep_result=False to the number of model points, the flux being
+        dropped as soon as it is complete (for consumers that only time or
+        count)."""
         if kind not in ('rr', 'ts'):
             raise ValueError("kind must be 'rr' or 'ts'")
         if ld not in _ldm.LAW_IDS:
             raise ValueError(f"unknown limb darkening law {ld}")
         req = Request(kind=kind, ld=ld, data=data, params=params)
+        req.state['keep'] = keep_result
         req.future = cf.Future()
         req.rid = next(self._ids)
         req.t_submit = time.perf_counter()
@@ -202,7 +208,7 @@ class RRServer:
 
     # -- scheduler ----------------------------------------------------------
     def _min_bytes(self, req):
-        if req.kind == 'ts' and req.nbytes > self.ts_chunk_bytes:
+        if req.kind == 'ts' and req.nbytes > self.ts_chunk_bytes and getattr(self.ex, 'result', 'host') == 'host':
             per_pv = req.nbytes / max(req.npv, 1)
             return int(per_pv * max(1, int(self.ts_chunk_bytes // per_pv)))
         return req.nbytes
@@ -266,6 +272,9 @@ class RRServer:
         if isinstance(result, Exception):
             req.future.set_exception(result)
         else:
+            if not req.state.get('keep', True):
+                req.state.pop('host_out', None)
+                result = req.points
             req.future.set_result(result)
 
     def _loop(self):
@@ -308,8 +317,13 @@ class GpuExecutor:
     MAX_REQ = 4096
     MAX_ITEMS = 65536
 
-    def __init__(self, device=None, nblocks=None):
+    def __init__(self, device=None, nblocks=None, result='host'):
+        """result='host': futures resolve to numpy arrays in pinned host memory;
+        'device': to CUDA tensors that stay on the GPU (for device-side consumers)."""
         import torch
+        if result not in ('host', 'device'):
+            raise ValueError("result must be 'host' or 'device'")
+        self.result = result
         from . import _lib
         from .rrmodel import RoadRunnerModel
         self.torch, self._lib = torch, _lib
@@ -473,6 +487,21 @@ class GpuExecutor:
         nz, ng = m.ze.size, m.ng
         ldf = (npt + 3) // 4 * 4
         chunk = g['chunk']
+        if self.result == 'device':
+            out = torch.empty((npv, npb, ldf), dtype=torch.float32, device=self.device)
+            wsb = L.rr_ts_workspace_bytes(1, npv, npb, ng)
+            ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
+            st = L.rr_ts_split(P(g['times_ff']), g['t_ref'], g['t_abs'], npt, P(g['k']), P(g['t0']), P(g['p']),
+                               P(g['a']), P(g['i']), P(g['e']), P(g['w']), npv, npb, int(h['nsamples'][0]),
+                               float(h['exptimes'][0]), P(g['ldp']), P(g['istar']), None, m.nk, ng, nz, m.dk,
+                               float(m.klims[0]), float(m.klims[1]), m.dg, P(tb['ze']), P(ws), wsb, P(out), ldf,
+                               self._lib.stream_ptr(self.device))
+            self._lib.check(st, "rr_ts_split")
+            ev = torch.cuda.Event()
+            ev.record(self.stream)
+            req.state['host_out'] = out[:, :, :npt]
+            req.state['ts_done_event'] = ev
+            return
         host = torch.empty((npv, npb, npt), dtype=torch.float32, pin_memory=True)
         req.state['host_out'] = host
         sp = self._lib.stream_ptr(self.device)
@@ -510,6 +539,10 @@ class GpuExecutor:
             req.state['copy_event'] = req.state['ts_done_event']
             return
         g = req.state['g']
+        if self.result == 'device':
+            req.state['host_out'] = g['flux'][:, :req.npt]
+            req.state['copy_event'] = req.state['last_event']
+            return
         host = torch.empty((req.npv, req.npt), dtype=torch.float32, pin_memory=True)
         self.copy_stream.wait_event(req.state['last_event'])
         with torch.cuda.stream(self.copy_stream):
@@ -523,7 +556,8 @@ class GpuExecutor:
         ev = req.state.get('copy_event')
         if ev is None or not ev.query():
             return None
-        return req.state['host_out'].numpy()
+        out = req.state['host_out']
+        return out if self.result == 'device' else out.numpy()
 
     def release(self, req):
         slot = req.state.pop('slot', None)
