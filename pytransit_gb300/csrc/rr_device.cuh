@@ -40,6 +40,22 @@ __device__ inline void tsort(R r1, R r2, R b, R& x, R& y, R& z) {
   }
 }
 
+// Overlap area of circles of radii r1, r2 at separation b in FP32, by the
+// kite form of Agol et al. 2020 (the stable counterpart of cci_acos;
+// circle_circle_intersection_area_kite, common.py:53-73, for any r1).
+__device__ inline float cci_kite_f32(float r1, float r2, float b) {
+  const float pi = 3.14159265358979f;
+  if (r1 < b - r2) return 0.0f;
+  if (r1 >= b + r2) return pi * r2 * r2;
+  if (b - r2 <= -r1) return pi * r1 * r1;
+  float x, y, w;
+  tsort<float>(r1, r2, b, x, y, w);
+  const float ak = 0.5f * sqrtf(fmaxf((x + (y + w)) * (w - (x - y)) * (w + (x - y)) * (x + (y - w)), 0.0f));
+  const float k0 = atan2f(2.0f * ak, (r2 - r1) * (r2 + r1) + b * b);
+  const float k1 = atan2f(2.0f * ak, (r1 - r2) * (r1 + r2) + b * b);
+  return r1 * r1 * k1 + r2 * r2 * k0 - ak;
+}
+
 // Area of the overlap of the unit stellar disk and a planet of radius k at
 // separation z: circle_circle_intersection_area_kite(1, k, z), common.py:53-73
 // (Agol et al. 2020).  kappa0 receives the second return value.

@@ -2,6 +2,7 @@
 // on the GPU: per-parameter-vector prologue kernels (limb-darkening means,
 // orbit + bounding box) and the per-point flux kernels, plain FP64 and split
 // precision.
+#include <algorithm>
 #include <cmath>
 
 #include "rr_device.cuh"
@@ -11,6 +12,7 @@ namespace rr {
 
 constexpr int LDM_PBB = 4;      // passbands per block of the LD-means kernel
 constexpr int MAX_NZ = 64;      // radial grid points staged in shared memory
+constexpr int LDM_SCRATCH = 2048;   // FP64 areas of the 2D table per chunk of rows (FP32 tables)
 
 // ---------------------------------------------------------------------------
 // Limb-darkening means, model_full.py:43-55:
@@ -19,11 +21,20 @@ constexpr int MAX_NZ = 64;      // radial grid points staged in shared memory
 // common.py:153-185) when k is outside [kmin, kmax] (mode 0) or when ik+1
 // would run past the table.  mode 1: the transmission-spectroscopy rule
 // kmin <= k <= kmax_pv[pv] (model_trspec.py:48); mode 2: always the 2D table.
-// One block per (pv, group of LDM_PBB passbands): the k-interpolated weight
-// slab is staged in shared memory with coalesced loads (rows padded to nz+1
-// words so the dot products are free of bank conflicts), then every (pb, g)
-// output is a dot product from shared memory.
+// One block per (pv, share of the passband groups): the k-interpolated weight
+// slab (or the 2D table, computed once per block) is staged in shared memory
+// with coalesced loads (rows padded to nz+1 words so the dot products are
+// free of bank conflicts), then the block walks its groups of LDM_PBB
+// passbands and every (pb, g) output is a dot product from shared memory:
+// ldm[pv][pb][g].
 // ---------------------------------------------------------------------------
+// Byte offset of the FP64 scratch after the slab [ng][nz+1] and the LD
+// profiles [LDM_PBB][MAX_NZ] (8-byte aligned).
+template <typename R>
+__host__ __device__ inline size_t ldm_scratch_offset(int ng, int nz) {
+  return (sizeof(R) * ((size_t)ng * (nz + 1) + (size_t)LDM_PBB * MAX_NZ) + 7) & ~size_t(7);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(128)
 ldm_kernel(const R* __restrict__ ldp, int npb, int nz, const double* __restrict__ kw, int kw_stride,
@@ -35,10 +46,6 @@ ldm_kernel(const R* __restrict__ ldp, int npb, int nz, const double* __restrict_
   R* l = Wk + (size_t)ng * (nz + 1);                       // [LDM_PBB][nz]
   const int ldw = nz + 1;
   const int pv = blockIdx.x;
-  const int pb0 = blockIdx.y * LDM_PBB;
-  const int nb = min(LDM_PBB, npb - pb0);
-  for (int i = threadIdx.x; i < nb * nz; i += blockDim.x)
-    l[i] = ldp[((size_t)pv * npb + pb0) * nz + i];
 
   const double k = kw[(size_t)pv * kw_stride];
   int ik = -1;
@@ -56,42 +63,73 @@ ldm_kernel(const R* __restrict__ ldp, int npb, int nz, const double* __restrict_
     for (int i = threadIdx.x; i < ng * nz; i += blockDim.x)
       Wk[(i / nz) * ldw + (i % nz)] = a0 * __ldg(W0 + i) + a1 * __ldg(W1 + i);
   } else {
-    // 2D table at this k, one row per thread in FP64: w_i = (A(ze_i) - A(ze_{i-1})) / sum
+    // 2D table at this k (calculate_weights_2d, common.py:153-185) in FP64:
+    // the areas A(ze_z) at every (g, z) in parallel, then per row the
+    // differences w_z = A(ze_z) - A(ze_{z-1}) and their sum, normalised.  The
+    // areas go to the table itself (FP64) or, for an FP32 table, to an FP64
+    // scratch in chunks of rows.
     const double gstep = (1.0 - 1e-7) / (double)(ng - 1);
-    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-      double gg = (double)g * gstep;
-      if (g == ng - 1) gg = 1.0 - 1e-7;
-      double bb = gg * (1.0 + k);
-      double a0 = cci_acos(ze[0], k, bb);
-      double s = a0;
-      R* row = Wk + (size_t)g * ldw;
-      row[0] = (R)a0;
-      for (int z = 1; z < nz; ++z) {
-        double a1 = cci_acos(ze[z], k, bb);
-        double wz = a1 - a0;
-        a0 = a1;
-        s += wz;
-        row[z] = (R)wz;
+    double* A2 = (sizeof(R) == 8) ? reinterpret_cast<double*>(Wk)
+                                  : reinterpret_cast<double*>(ldm_smem + ldm_scratch_offset<R>(ng, nz));
+    const int rows = (sizeof(R) == 8) ? ng : max(1, LDM_SCRATCH / nz);
+    const int lda = (sizeof(R) == 8) ? ldw : nz;
+    for (int g0 = 0; g0 < ng; g0 += rows) {
+      const int nr = min(rows, ng - g0);
+      for (int i = threadIdx.x; i < nr * nz; i += blockDim.x) {
+        const int g = g0 + i / nz, z = i % nz;
+        const double gg = (g == ng - 1) ? 1.0 - 1e-7 : (double)g * gstep;
+        A2[(size_t)(i / nz) * lda + z] = cci_acos(ze[z], k, gg * (1.0 + k));
       }
-      // normalise in FP64 from the stored differences (exact for R = double)
-      for (int z = 0; z < nz; ++z) row[z] = (R)((double)row[z] / s);
+      __syncthreads();
+      for (int rr = threadIdx.x; rr < nr; rr += blockDim.x) {
+        const double* a = A2 + (size_t)rr * lda;
+        R* row = Wk + (size_t)(g0 + rr) * ldw;
+        double s = a[0];
+        for (int z = 1; z < nz; ++z) s += a[z] - a[z - 1];
+        // in place for an FP64 table: walk down so a[z-1] is still the area
+        for (int z = nz - 1; z >= 1; --z) row[z] = (R)((a[z] - a[z - 1]) / s);
+        row[0] = (R)(a[0] / s);
+      }
+      __syncthreads();
     }
   }
-  __syncthreads();
-  R* out = ldm + ((size_t)pv * npb + pb0) * ng;
-  for (int j = threadIdx.x; j < nb * ng; j += blockDim.x) {
-    const int b = j / ng, g = j % ng;
-    const R* row = Wk + (size_t)g * ldw;
-    const R* lb = l + b * nz;
-    R d = R(0);
-    for (int z = 0; z < nz; ++z) d += row[z] * lb[z];
-    out[(size_t)b * ng + g] = d;
+  const int ngroups = (npb + LDM_PBB - 1) / LDM_PBB;
+  for (int grp = blockIdx.y; grp < ngroups; grp += gridDim.y) {
+    const int pb0 = grp * LDM_PBB;
+    const int nb = min(LDM_PBB, npb - pb0);
+    __syncthreads();   // the slab is complete; the previous group's l is no longer read
+    for (int i = threadIdx.x; i < nb * nz; i += blockDim.x)
+      l[i] = ldp[((size_t)pv * npb + pb0) * nz + i];
+    __syncthreads();
+    for (int j = threadIdx.x; j < nb * ng; j += blockDim.x) {
+      const int b = j / ng, g = j % ng;
+      const R* row = Wk + (size_t)g * ldw;
+      const R* lb = l + b * nz;
+      R d = R(0);
+      for (int z = 0; z < nz; ++z) d += row[z] * lb[z];
+      ldm[((size_t)pv * npb + pb0 + b) * ng + g] = d;
+    }
   }
 }
 
+// Blocks per pv of the LD-means kernel: the 2D table (mode 2) is costly FP64
+// work (GB300's FP64 rate is 1/64 of FP32), built once per block, so all of a
+// pv's passbands share one block; the 3D slab is a cheap lerp.
+static dim3 ldm_grid(int npv, int npb, int mode) {
+  const int ngroups = (npb + LDM_PBB - 1) / LDM_PBB;
+  const int want = (mode == 2) ? 1 : (4096 + npv - 1) / npv;
+  return dim3(npv, (unsigned)std::max(1, std::min(ngroups, want)));
+}
+
+// Dynamic shared memory of ldm_kernel<R>; above the default 48 KB (large ng)
+// the kernel is opted in to the larger carve-out first.
 template <typename R>
 static size_t ldm_smem_bytes(int ng, int nz) {
-  return sizeof(R) * ((size_t)ng * (nz + 1) + (size_t)LDM_PBB * nz);
+  const size_t scratch = (sizeof(R) == 8) ? 0 : sizeof(double) * LDM_SCRATCH;
+  const size_t bytes = ldm_scratch_offset<R>(ng, nz) + scratch;
+  if (bytes > 48 * 1024)
+    cudaFuncSetAttribute(ldm_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return bytes;
 }
 
 // Host launchers of the LD-means kernel for the other translation units.
@@ -99,9 +137,8 @@ template <typename R>
 static void launch_ldm_impl(const R* ldp, int npv, int npb, int nz, const double* kw, int kw_stride, const R* W,
                             int nk, int ng, double dk, double kmin, double kmax, const double* ze, int mode,
                             const double* kmax_pv, R* ldm, cudaStream_t s) {
-  dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-  ldm_kernel<R><<<lg, 128, ldm_smem_bytes<R>(ng, nz), s>>>(ldp, npb, nz, kw, kw_stride, W, nk, ng, dk, kmin, kmax,
-                                                          ze, mode, kmax_pv, ldm);
+  ldm_kernel<R><<<ldm_grid(npv, npb, mode), 128, ldm_smem_bytes<R>(ng, nz), s>>>(
+      ldp, npb, nz, kw, kw_stride, W, nk, ng, dk, kmin, kmax, ze, mode, kmax_pv, ldm);
 }
 void launch_ldm_f32(const float* ldp, int npv, int npb, int nz, const double* kw, int kw_stride, const float* W,
                     int nk, int ng, double dk, double kmin, double kmax, const double* ze, int mode,
@@ -788,9 +825,8 @@ int rr_prepare_f64(const double* k, int nkc, const double* p, const double* a, c
     ldm_basis_kernel<double><<<npv, 128, sizeof(double) * npb * nb, s>>>(
         law, ldc, npar, npb, k, nkc, basis, nb, nk, ng, dk, kmin, kmax, ldp, nz, z_edges, ldm);
   } else {
-    dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-    ldm_kernel<double><<<lg, 128, ldm_smem_bytes<double>(ng, nz), s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk,
-                                                                       kmin, kmax, z_edges, 0, nullptr, ldm);
+    ldm_kernel<double><<<ldm_grid(npv, npb, 0), 128, ldm_smem_bytes<double>(ng, nz), s>>>(
+        ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0, nullptr, ldm);
   }
   OrbitArgs oa{};
   oa.k = k; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w;
@@ -858,9 +894,8 @@ int rr_prepare_split(double t_ref, double t_absmax, const double* k, int nkc, co
     ldm_basis_kernel<float><<<npv, 128, sizeof(float) * npb * nb, s>>>(
         law, ldc, npar, npb, k, nkc, basis, nb, nk, ng, dk, kmin, kmax, ldp, nz, z_edges, t.ldm);
   } else {
-    dim3 lg(npv, (npb + LDM_PBB - 1) / LDM_PBB);
-    ldm_kernel<float><<<lg, 128, ldm_smem_bytes<float>(ng, nz), s>>>(ldp, npb, nz, k, nkc, weights, nk, ng, dk,
-                                                                     kmin, kmax, z_edges, 0, nullptr, t.ldm);
+    ldm_kernel<float><<<ldm_grid(npv, npb, 0), 128, ldm_smem_bytes<float>(ng, nz), s>>>(
+        ldp, npb, nz, k, nkc, weights, nk, ng, dk, kmin, kmax, z_edges, 0, nullptr, t.ldm);
   }
   OrbitArgs oa{};
   oa.k = k; oa.t0 = t0; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w; oa.exptimes = exptimes;

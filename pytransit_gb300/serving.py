@@ -23,6 +23,7 @@ scheduler thread owns the GPU:
 The GPU work is behind ``GpuExecutor`` so that the scheduling logic can be
 exercised on the CPU with a fake executor (tests/test_serving_cpu.py).
 """
+import bisect
 import collections
 import concurrent.futures as cf
 import ctypes as C
@@ -129,6 +130,90 @@ def request_bytes(req: Request, ng: int = 100, nz: int = 40) -> int:
     return int(data + params + tables + out)
 
 
+def _layout(parts):
+    """Byte offsets (256-byte aligned) of named parts in one buffer, and its size."""
+    off, cur = {}, 0
+    for name, nbytes in parts:
+        cur = (cur + 255) & ~255
+        off[name] = cur
+        cur += int(nbytes)
+    return off, max(cur, 256)
+
+
+class _DeviceArena:
+    """The serving loop's device memory: one allocation made when the server
+    starts, sized to the HBM budget plus headroom, from which every admitted
+    request takes one contiguous block (first fit, 256-byte aligned, freed
+    blocks merged with their neighbours).  No cudaMalloc/cudaFree while
+    serving."""
+
+    def __init__(self, torch, device, nbytes):
+        self.size = int(nbytes) & ~255
+        self.buf = torch.empty(self.size, dtype=torch.uint8, device=device)
+        self.base = self.buf.data_ptr()
+        self.free_list = [(0, self.size)]     # (offset, size), sorted by offset
+        self.used = 0
+
+    def alloc(self, n):
+        n = (int(n) + 255) & ~255
+        for j, (o, sz) in enumerate(self.free_list):
+            if sz >= n:
+                if sz == n:
+                    del self.free_list[j]
+                else:
+                    self.free_list[j] = (o + n, sz - n)
+                self.used += n
+                return o
+        return None
+
+    def free(self, o, n):
+        n = (int(n) + 255) & ~255
+        self.used -= n
+        fl = self.free_list
+        j = bisect.bisect_left(fl, (o, 0))
+        fl.insert(j, (o, n))
+        if j + 1 < len(fl) and fl[j][0] + fl[j][1] == fl[j + 1][0]:
+            fl[j] = (fl[j][0], fl[j][1] + fl[j + 1][1])
+            del fl[j + 1]
+        if j > 0 and fl[j - 1][0] + fl[j - 1][1] == fl[j][0]:
+            fl[j - 1] = (fl[j - 1][0], fl[j - 1][1] + fl[j][1])
+            del fl[j]
+
+
+class _PinnedRing:
+    """Pinned host staging for request uploads, used as a ring: a region is
+    handed out again once the event recorded after its copy has completed."""
+
+    def __init__(self, torch, nbytes):
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        self.np = self.buf.numpy()
+        self.size = nbytes
+        self.head = 0
+        self.live = collections.deque()       # (start, end, event) in allocation order
+
+    def alloc(self, n):
+        """Offset of n free bytes, or None if n does not fit the ring."""
+        n = (n + 255) & ~255
+        if n > self.size:
+            return None
+        if self.head + n > self.size:
+            self.head = 0
+        lo, hi = self.head, self.head + n
+        last = None
+        for a, b, ev in self.live:
+            if a < hi and lo < b:
+                last = ev
+        if last is not None:
+            last.synchronize()
+        while self.live and self.live[0][2].query():
+            self.live.popleft()
+        self.head = hi
+        return lo
+
+    def commit(self, lo, n, event):
+        self.live.append((lo, lo + ((n + 255) & ~255), event))
+
+
 def work_items(npv: int, npt: int, target_tiles: int = 256):
     """(pv0, pv1, tile0, tile1) chunks of about target_tiles pv-tiles each."""
     ntiles = max(1, (npt + TILE - 1) // TILE)
@@ -144,7 +229,8 @@ class RRServer:
 
     def __init__(self, executor=None, hbm_budget: float = 120e9, step_items: int = 4096,
                  ts_chunk_bytes: float = 4e9, device=None, result: str = 'host'):
-        self.ex = executor if executor is not None else GpuExecutor(device, result=result)
+        self.ex = executor if executor is not None else GpuExecutor(
+            device, result=result, arena_bytes=int(hbm_budget * 1.1) + (1 << 30))
         self.budget = int(hbm_budget)
         self.step_items = step_items
         self.ts_chunk_bytes = ts_chunk_bytes
@@ -152,6 +238,8 @@ class RRServer:
         self._ids = itertools.count()
         self._queue = collections.deque()
         self._active = collections.OrderedDict()
+        self._issued = collections.OrderedDict()     # all GPU work enqueued, result pending
+        self._ts_new = []
         self._used = 0
         self._cv = threading.Condition()
         self._stop = False
@@ -214,27 +302,36 @@ class RRServer:
         return req.nbytes
 
     def _admit(self):
-        admitted = []
-        with self._cv:
-            while self._queue:
+        """Admit queued requests in order while the budget allows; a request
+        the executor cannot place yet (device memory fragmented) waits at
+        the head of the queue for the next completion."""
+        while True:
+            with self._cv:
+                if not self._queue:
+                    return
                 req = self._queue[0]
                 need = self._min_bytes(req)
                 if self._used + need > self.budget:
-                    break
+                    return
                 self._queue.popleft()
                 self._used += need
                 req.state['held'] = need
                 self.stats.peak_bytes = max(self.stats.peak_bytes, self._used)
-                admitted.append(req)
-        for req in admitted:
             req.t_admit = time.perf_counter()
             try:
-                self.ex.setup(req, self.ts_chunk_bytes)
+                placed = self.ex.setup(req, self.ts_chunk_bytes)
             except Exception as exc:   # pragma: no cover - surfaced to the client
                 self._finish(req, exc)
                 continue
+            if placed is False:
+                with self._cv:
+                    self._used -= req.state.pop('held')
+                    self._queue.appendleft(req)
+                return
             if req.kind == 'rr':
                 req.state['items'] = collections.deque(work_items(req.npv, req.npt))
+            else:
+                self._ts_new.append(req)
             with self._cv:
                 self._active[req.rid] = req
                 self.stats.admitted += 1
@@ -287,23 +384,29 @@ class RRServer:
                     continue
             self._admit()
             batch = self._take_items()
-            ts_work = [r for r in list(self._active.values()) if r.kind == 'ts' and not r.state.get('ts_issued')]
+            ts_work, self._ts_new = self._ts_new, []
             if batch or ts_work:
                 self.ex.step(batch, ts_work)
                 self.stats.steps += 1
                 for r in ts_work:
-                    r.state['ts_issued'] = True
+                    self._issued[r.rid] = r
                 for r in {id(r): r for r, _ in batch}.values():
                     if not r.state['items']:
-                        r.state['issued'] = True
-            for r in list(self._active.values()):
-                if (r.kind == 'rr' and r.state.get('issued')) or (r.kind == 'ts' and r.state.get('ts_issued')):
-                    if not r.state.get('copy_started'):
-                        self.ex.start_copy(r)
-                        r.state['copy_started'] = True
-                    done = self.ex.poll_copy(r)
-                    if done is not None:
-                        self._finish(r, done)
+                        self._issued[r.rid] = r
+            # completions, polled in issue order: stop at the few oldest still running
+            pending = 0
+            for r in list(self._issued.values()):
+                if not r.state.get('copy_started'):
+                    self.ex.start_copy(r)
+                    r.state['copy_started'] = True
+                done = self.ex.poll_copy(r)
+                if done is not None:
+                    del self._issued[r.rid]
+                    self._finish(r, done)
+                else:
+                    pending += 1
+                    if pending >= 4:
+                        break
             if not batch and not ts_work:
                 time.sleep(0.0002)
         self.ex.shutdown()
@@ -317,9 +420,11 @@ class GpuExecutor:
     MAX_REQ = 4096
     MAX_ITEMS = 65536
 
-    def __init__(self, device=None, nblocks=None, result='host'):
+    def __init__(self, device=None, nblocks=None, result='host', arena_bytes=None):
         """result='host': futures resolve to numpy arrays in pinned host memory;
-        'device': to CUDA tensors that stay on the GPU (for device-side consumers)."""
+        'device': to CUDA tensors that stay on the GPU (for device-side consumers).
+        arena_bytes: device memory reserved for requests (default: 90 % of
+        what is free)."""
         import torch
         if result not in ('host', 'device'):
             raise ValueError("result must be 'host' or 'device'")
@@ -334,8 +439,16 @@ class GpuExecutor:
                                                 C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
         self.L.rr_full_split_tables.restype = None
         self.L.rr_serve_flux_split.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p]
-        self.stream = torch.cuda.Stream(self.device)
+        self.stream = torch.cuda.Stream(self.device)          # batched steps (graph replays)
+        self.setup_stream = torch.cuda.Stream(self.device)    # per-request uploads and prologues
         self.copy_stream = torch.cuda.Stream(self.device)
+        self.ts_streams = [torch.cuda.Stream(self.device) for _ in range(4)]
+        self._ts_next = 0
+        self._sp_setup = self.setup_stream.cuda_stream
+        self.ring = _PinnedRing(torch, 256 << 20)
+        free_b = torch.cuda.mem_get_info(self.device)[0]
+        want = int(0.9 * free_b) if arena_bytes is None else int(arena_bytes)
+        self.arena = _DeviceArena(torch, self.device, max(1 << 20, min(want, free_b - (2 << 30))))
         # shared tables: one model per law (weight table, grids, basis tables)
         self.models = {}
         self._RR = RoadRunnerModel
@@ -351,22 +464,32 @@ class GpuExecutor:
         self.L.rr_serve_struct_sizes(C.byref(rs), C.byref(is_))
         if rs.value != self.desc_dtype.itemsize or is_.value != 24:
             raise RuntimeError("rr_serve_request / rr_serve_item layout mismatch with the library")
-        self.descs_h = np.zeros(self.MAX_REQ, self.desc_dtype)
-        self.descs_d = torch.zeros(self.MAX_REQ * self.desc_dtype.itemsize, dtype=torch.uint8, device=self.device)
-        self.items_pin = torch.zeros(self.MAX_ITEMS * 6 + 8, dtype=torch.int32, pin_memory=True)
+        # descriptors: a pinned host mirror written at set-up, copied (dirty
+        # slot range only, asynchronously, in stream order) before a step
+        dsz = self.MAX_REQ * self.desc_dtype.itemsize
+        self.descs_pin = torch.zeros(dsz, dtype=torch.uint8, pin_memory=True)
+        self.descs_h = self.descs_pin.numpy().view(self.desc_dtype)
+        self.descs_d = torch.zeros(dsz, dtype=torch.uint8, device=self.device)
+        self._dirty = set()
+        # item list: two pinned staging buffers used in turn; a buffer is
+        # rewritten once the copy that last read it has run
+        self.items_pin = [torch.zeros(self.MAX_ITEMS * 6 + 8, dtype=torch.int32, pin_memory=True) for _ in range(2)]
+        self.items_ev = [None, None]
+        self._istep = 0
         self.items_d = torch.zeros(self.MAX_ITEMS * 6 + 8, dtype=torch.int32, device=self.device)
         self.counter = torch.zeros(4, dtype=torch.int32, device=self.device)
         self.free_slots = list(range(self.MAX_REQ - 1, -1, -1))
         self.graph = None
-        self.step_events = collections.deque()
         self._capture()
 
     # -- helpers -------------------------------------------------------------
     def _model(self, ld):
         if ld not in self.models:
             m = self._RR(ld, precision='split', device=self.device)
-            with self.torch.cuda.stream(self.stream):
-                m._device_tables(self.device)
+            with self.torch.cuda.stream(self.setup_stream):     # ordered before the set-ups that use them
+                tb = m.tables = m._device_tables(self.device)
+            for n in ('mu', 'ze', 'W32'):
+                tb[n + '_ptr'] = tb[n].data_ptr()
             self.models[ld] = m
         return self.models[ld]
 
@@ -375,8 +498,7 @@ class GpuExecutor:
         torch = self.torch
         P = self._lib.ptr
         nitems_ptr = C.c_void_p(self.items_d.data_ptr() + self.MAX_ITEMS * 6 * 4)
-        self.items_pin[self.MAX_ITEMS * 6] = 0
-        self.items_d.copy_(self.items_pin)
+        self.items_d.zero_()
         torch.cuda.synchronize(self.device)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, stream=self.stream):
@@ -388,150 +510,210 @@ class GpuExecutor:
         self.graph = g
 
     # -- request set-up ---------------------------------------------------------
+    _INPUTS = (('time', 'time'), ('exptimes', 'exptimes'), ('k', 'k'), ('t0', 't0'), ('p', 'p'), ('a', 'a'),
+               ('i', 'i'), ('e', 'e'), ('w', 'w'), ('ldc', 'ldc'), ('lcids', 'lcids'), ('pbids', 'pbids'),
+               ('epids', 'epids'), ('nsamples', 'nsamples'))
+
     def setup(self, req, ts_chunk_bytes):
-        torch, L, P = self.torch, self.L, self._lib.ptr
+        """Everything a request keeps on the device lives in one allocation:
+        its inputs (staged in the pinned ring, one host-to-device copy), the
+        FP32-pair times, LD tables, prologue workspace and output."""
+        torch, L = self.torch, self.L
         h = req.state['host']
         m = self._model(req.ld)
-        tb = m.tables = m._device_tables(self.device)
-        dev = self.device
-        with torch.cuda.stream(self.stream):
-            sp = self._lib.stream_ptr(dev)
-            g = {}
-            for n in ('time', 'exptimes', 'k', 't0', 'p', 'a', 'i', 'e', 'w', 'ldc'):
-                g[n] = torch.as_tensor(np.array(h[n])).pin_memory().to(dev, non_blocking=True)
-            for n in ('lcids', 'pbids', 'epids', 'nsamples'):
-                g[n] = torch.as_tensor(np.array(h[n])).pin_memory().to(dev, non_blocking=True)
-            npt, npv, npb, nlc = req.npt, req.npv, h['npb'], h['nlc']
-            tmin, tmax = float(h['time'].min()), float(h['time'].max())
-            t_ref = 0.5 * (tmin + tmax)
-            t_abs = max(tmax - t_ref, t_ref - tmin)
-            g['times_ff'] = torch.empty(max(int(L.rr_time_split_floats(npt)), 4), dtype=torch.float32, device=dev)
-            self._lib.check(L.rr_time_split(P(g['time']), P(g['lcids']), npt, t_ref, P(g['times_ff']), sp))
-            nz, ng = m.ze.size, m.ng
-            npar = h['ldc'].shape[2]
-            g['ldp'] = torch.empty((npv, npb, nz), dtype=torch.float32, device=dev)
-            g['istar'] = torch.empty((npv, npb), dtype=torch.float32, device=dev)
-            self._lib.check(L.rr_ld_tables_f32(m.ld_law, P(g['ldc']), npv, npb, npar, P(tb['mu']), nz, P(g['ldp']),
-                                               P(g['istar']), sp))
-            ldf = (npt + 3) // 4 * 4
+        tb = m.tables
+        npt, npv, npb, nlc = req.npt, req.npv, h['npb'], h['nlc']
+        nz, ng = m.ze.size, m.ng
+        npar = h['ldc'].shape[2]
+        ldf = (npt + 3) // 4 * 4
+        arrays = [(name, h[key]) for name, key in self._INPUTS]
+        parts = [(name, a.nbytes) for name, a in arrays]
+        n_in = _layout(parts)[1]
+        parts += [('times_ff', 4 * max(int(L.rr_time_split_floats(npt)), 4)), ('ldp', 4 * npv * npb * nz),
+                  ('istar', 4 * npv * npb)]
+        if req.kind == 'rr':
+            nep = h['t0'].shape[1]
+            wsb = int(L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng))
+            parts += [('ws', wsb), ('flux', 4 * npv * ldf)]
+        else:
+            per_pv = max(1, req.nbytes // max(npv, 1))
+            chunk = npv if self.result == 'device' else max(1, min(npv, int(ts_chunk_bytes // per_pv)))
+            wsb = int(L.rr_ts_workspace_bytes(1, chunk, npb, ng))
+            parts += [('ws', wsb)]
+            if self.result == 'device':
+                parts += [('flux', 4 * npv * npb * ldf)]
+        # a result handed to the caller on the device is a tensor of its own;
+        # everything else lives in the request's arena block
+        own_flux = self.result == 'device' and req.state.get('keep', True) and 'flux' in dict(parts)
+        if own_flux:
+            flux_bytes = dict(parts)['flux']
+            parts = [pt for pt in parts if pt[0] != 'flux']
+        off, total = _layout(parts)
+        blk = self.arena.alloc(total)
+        if blk is None:
+            if total > self.arena.size or self.arena.used == 0:
+                raise MemoryError(f"request {req.rid} needs {total / 1e9:.2f} GB of device memory, more than the "
+                                  f"{self.arena.size / 1e9:.2f} GB arena")
+            return False
+        lo = self.ring.alloc(n_in)
+        if lo is None:                 # larger than the ring: a pinned buffer of its own
+            stage = torch.empty(n_in, dtype=torch.uint8, pin_memory=True)
+            sv, lo = stage.numpy(), 0
+        else:
+            stage, sv = self.ring.buf, self.ring.np
+        for name, a in arrays:
+            o = lo + off[name]
+            sv[o:o + a.nbytes] = np.ascontiguousarray(a).reshape(-1).view(np.uint8)
+        tmin, tmax = float(h['time'].min()), float(h['time'].max())
+        t_ref = 0.5 * (tmin + tmax)
+        t_abs = max(tmax - t_ref, t_ref - tmin)
+        sp = self._sp_setup
+        with torch.cuda.stream(self.setup_stream):
+            buf = self.arena.buf[blk:blk + total]
+            base = self.arena.base + blk
+            P = {name: base + o for name, o in off.items()}
+            if own_flux:
+                fl = torch.empty(flux_bytes // 4, dtype=torch.float32, device=self.device)
+                P['flux'] = fl.data_ptr()
+            buf[:n_in].copy_(stage[lo:lo + n_in], non_blocking=True)
+            self._lib.check(L.rr_time_split(P['time'], P['lcids'], npt, t_ref, P['times_ff'], sp))
+            self._lib.check(L.rr_ld_tables_f32(m.ld_law, P['ldc'], npv, npb, npar, tb['mu_ptr'], nz, P['ldp'],
+                                               P['istar'], sp))
+            g = dict(P=P, t_ref=t_ref, t_abs=t_abs, wsb=wsb, block=(blk, total))
             if req.kind == 'rr':
-                nep = h['t0'].shape[1]
-                basis, nb = m._basis(dev, npar, True)
-                wsb = L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng)
-                g['ws'] = torch.empty(wsb, dtype=torch.uint8, device=dev)
+                basis, nb = m._basis(self.device, npar, True)
                 self._lib.check(L.rr_prepare_split(
-                    t_ref, t_abs, P(g['k']), h['k'].shape[1], P(g['t0']), nep, nep, P(g['p']), P(g['a']),
-                    P(g['i']), P(g['e']), P(g['w']), npv, nlc, npb, P(g['pbids']), P(g['epids']),
-                    P(g['nsamples']), P(g['exptimes']), P(g['ldp']), P(g['istar']), P(tb['W32']), m.nk, ng, nz,
-                    m.dk, float(m.klims[0]), float(m.klims[1]), P(tb['ze']), P(g['ws']), wsb, sp, m.ld_law,
-                    P(g['ldc']), npar, P(basis), nb))
-                g['flux'] = torch.empty((npv, ldf), dtype=torch.float32, device=dev)
+                    t_ref, t_abs, P['k'], h['k'].shape[1], P['t0'], nep, nep, P['p'], P['a'], P['i'], P['e'],
+                    P['w'], npv, nlc, npb, P['pbids'], P['epids'], P['nsamples'], P['exptimes'], P['ldp'],
+                    P['istar'], tb['W32_ptr'], m.nk, ng, nz, m.dk, m.klims[0], m.klims[1], tb['ze_ptr'], P['ws'],
+                    wsb, sp, m.ld_law, P['ldc'], npar, None if basis is None else basis.data_ptr(), nb))
+                g['flux'] = (fl if own_flux else buf[off['flux']:off['flux'] + 4 * npv * ldf].view(torch.float32)
+                             ).view(npv, ldf)
                 orb, lc, ldm = C.c_void_p(), C.c_void_p(), C.c_void_p()
-                L.rr_full_split_tables(C.c_void_p(g['ws'].data_ptr()), npv, npb, nlc, nep, ng, C.byref(orb),
-                                       C.byref(lc), C.byref(ldm))
+                L.rr_full_split_tables(P['ws'], npv, npb, nlc, nep, ng, C.byref(orb), C.byref(lc), C.byref(ldm))
                 slot = self.free_slots.pop()
                 req.state['slot'] = slot
                 d = self.descs_h[slot]
-                d['times_ff'], d['lcids'] = g['times_ff'].data_ptr(), g['lcids'].data_ptr()
+                d['times_ff'], d['lcids'] = P['times_ff'], P['lcids']
                 d['orb32'], d['lc32'], d['ldm'] = orb.value, lc.value, ldm.value
-                d['flux'], d['ldflux'] = g['flux'].data_ptr(), ldf
+                d['flux'], d['ldflux'] = P['flux'], ldf
                 d['npt'], d['npv'], d['nlc'], d['npb'], d['ng'] = npt, npv, nlc, npb, ng
                 d['inv_dg'] = np.float32(1.0 / m.dg)
-                req.state['desc_dirty'] = True
+                self._dirty.add(slot)
             else:
-                g['t_ref'], g['t_abs'] = t_ref, t_abs
-                per_pv = max(1, req.nbytes // max(npv, 1))
-                g['chunk'] = max(1, min(npv, int(ts_chunk_bytes // per_pv)))
-            req.state['g'] = g
-            req.state['model'] = m
+                g['chunk'] = chunk
+                if self.result == 'device':
+                    n = 4 * npv * npb * ldf
+                    g['flux'] = (fl if own_flux else buf[off['flux']:off['flux'] + n].view(torch.float32)
+                                 ).view(npv, npb, ldf)
+        ready = torch.cuda.Event()
+        ready.record(self.setup_stream)
+        if stage is self.ring.buf:
+            self.ring.commit(lo, n_in, ready)
+        else:
+            g['stage'] = stage
+        g['ready'] = ready
+        req.state['g'] = g
+        req.state['model'] = m
 
     # -- steps -------------------------------------------------------------------
     def step(self, batch, ts_reqs):
         torch = self.torch
         with torch.cuda.stream(self.stream):
             if batch:
-                dirty = [r for r, _ in batch if r.state.pop('desc_dirty', False)]
-                if dirty:
-                    self.descs_d.copy_(torch.from_numpy(self.descs_h.view(np.uint8)), non_blocking=False)
-                # the staging buffer is reused: wait for the previous step's copy
-                while self.step_events and len(self.step_events) > 1:
-                    self.step_events.popleft().synchronize()
-                if self.step_events:
-                    self.step_events[-1].synchronize()
-                arr = self.items_pin.numpy()
+                for r in {id(r): r for r, _ in batch}.values():
+                    g = r.state['g']
+                    if not g.get('waited'):
+                        self.stream.wait_event(g['ready'])
+                        g['waited'] = True
+                if self._dirty:
+                    lo, hi = min(self._dirty), max(self._dirty) + 1
+                    isz = self.desc_dtype.itemsize
+                    self.descs_d[lo * isz:hi * isz].copy_(self.descs_pin[lo * isz:hi * isz], non_blocking=True)
+                    self._dirty.clear()
+                j = self._istep % 2
+                self._istep += 1
+                if self.items_ev[j] is not None:
+                    self.items_ev[j].synchronize()
+                pin = self.items_pin[j]
+                arr = pin.numpy()
                 n = len(batch)
-                it = np.array([(r.state['slot'], *w, 0) for r, w in batch], np.int32).reshape(-1)
-                arr[:n * 6] = it
-                arr[self.MAX_ITEMS * 6] = n
-                self.items_d[:n * 6].copy_(self.items_pin[:n * 6], non_blocking=True)
-                self.items_d[self.MAX_ITEMS * 6:self.MAX_ITEMS * 6 + 1].copy_(
-                    self.items_pin[self.MAX_ITEMS * 6:self.MAX_ITEMS * 6 + 1], non_blocking=True)
+                arr[:n * 6] = np.array([(r.state['slot'], *w, 0) for r, w in batch], np.int32).reshape(-1)
+                arr[n * 6] = n
+                # items and their count in one copy; the count goes to its fixed slot
+                self.items_d[:n * 6].copy_(pin[:n * 6], non_blocking=True)
+                self.items_d[self.MAX_ITEMS * 6:self.MAX_ITEMS * 6 + 1].copy_(pin[n * 6:n * 6 + 1], non_blocking=True)
+                cev = torch.cuda.Event()
+                cev.record(self.stream)
+                self.items_ev[j] = cev
                 self.graph.replay()
-            for r in ts_reqs:
-                self._run_ts(r)
             ev = torch.cuda.Event()
             ev.record(self.stream)
-            self.step_events.append(ev)
             for r, _ in batch:
                 r.state['last_event'] = ev
-            for r in ts_reqs:
-                r.state['last_event'] = ev
+        # transmission-spectroscopy requests run as their own launches on a
+        # few side streams, overlapping the batched step and one another
+        for r in ts_reqs:
+            self._run_ts(r, self.ts_streams[self._ts_next % len(self.ts_streams)])
+            self._ts_next += 1
 
-    def _run_ts(self, req):
-        """Transmission-spectroscopy request in parameter-vector chunks; each
-        chunk is copied to the host result as soon as it is computed."""
-        torch, L, P = self.torch, self.L, self._lib.ptr
+    def _run_ts(self, req, stream):
+        """Transmission-spectroscopy request on one of the TS streams; with
+        host results in parameter-vector chunks, each chunk copied to the host
+        result as soon as it is computed."""
+        torch, L = self.torch, self.L
         g, h, m = req.state['g'], req.state['host'], req.state['model']
+        base = g['P']
+
+        def P(name, elems=0, size=8):
+            return base[name] + elems * size
+
         tb = m.tables
         npv, npt, npb = req.npv, req.npt, h['npb']
         nz, ng = m.ze.size, m.ng
         ldf = (npt + 3) // 4 * 4
-        chunk = g['chunk']
-        if self.result == 'device':
-            out = torch.empty((npv, npb, ldf), dtype=torch.float32, device=self.device)
-            wsb = L.rr_ts_workspace_bytes(1, npv, npb, ng)
-            ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
-            st = L.rr_ts_split(P(g['times_ff']), g['t_ref'], g['t_abs'], npt, P(g['k']), P(g['t0']), P(g['p']),
-                               P(g['a']), P(g['i']), P(g['e']), P(g['w']), npv, npb, int(h['nsamples'][0]),
-                               float(h['exptimes'][0]), P(g['ldp']), P(g['istar']), None, m.nk, ng, nz, m.dk,
-                               float(m.klims[0]), float(m.klims[1]), m.dg, P(tb['ze']), P(ws), wsb, P(out), ldf,
-                               self._lib.stream_ptr(self.device))
-            self._lib.check(st, "rr_ts_split")
-            ev = torch.cuda.Event()
-            ev.record(self.stream)
-            req.state['host_out'] = out[:, :, :npt]
-            req.state['ts_done_event'] = ev
-            return
-        host = torch.empty((npv, npb, npt), dtype=torch.float32, pin_memory=True)
-        req.state['host_out'] = host
-        sp = self._lib.stream_ptr(self.device)
-        wsb = L.rr_ts_workspace_bytes(1, chunk, npb, ng)
-        ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
-        outs = [torch.empty((chunk, npb, ldf), dtype=torch.float32, device=self.device) for _ in range(2)]
-        for o in outs:
-            o.record_stream(self.copy_stream)
-        for j, pv0 in enumerate(range(0, npv, chunk)):
-            n = min(chunk, npv - pv0)
-            out = outs[j % 2]
-            if j >= 2:
-                # the buffer's previous chunk must have left for the host
-                self.stream.wait_event(req.state['chunk_ev'][j % 2])
-            off8 = lambda t, w=1: C.c_void_p(t.data_ptr() + pv0 * w * t.element_size())
-            st = L.rr_ts_split(P(g['times_ff']), g['t_ref'], g['t_abs'], npt, off8(g['k'], npb), off8(g['t0']),
-                               off8(g['p']), off8(g['a']), off8(g['i']), off8(g['e']), off8(g['w']), n, npb,
-                               int(h['nsamples'][0]), float(h['exptimes'][0]), off8(g['ldp'], npb * nz),
-                               off8(g['istar'], npb), None, m.nk, ng, nz, m.dk, float(m.klims[0]),
-                               float(m.klims[1]), m.dg, P(tb['ze']), P(ws), wsb, P(out), ldf, sp)
-            self._lib.check(st, "rr_ts_split")
-            ev = torch.cuda.Event()
-            ev.record(self.stream)
-            self.copy_stream.wait_event(ev)
-            with torch.cuda.stream(self.copy_stream):
-                host[pv0:pv0 + n].copy_(out[:n, :, :npt], non_blocking=True)
-                cev = torch.cuda.Event()
-                cev.record(self.copy_stream)
-            req.state.setdefault('chunk_ev', [None, None])[j % 2] = cev
-        req.state['ts_done_event'] = cev
+        ns0, ex0 = int(h['nsamples'][0]), float(h['exptimes'][0])
+        stream.wait_event(g['ready'])        # set-up kernels of this request
+        with torch.cuda.stream(stream):
+            sp = self._lib.stream_ptr(self.device)
+
+            def launch(pv0, n, out_ptr):
+                st = L.rr_ts_split(P('times_ff'), g['t_ref'], g['t_abs'], npt, P('k', pv0 * npb), P('t0', pv0),
+                                   P('p', pv0), P('a', pv0), P('i', pv0), P('e', pv0), P('w', pv0), n, npb, ns0,
+                                   ex0, P('ldp', pv0 * npb * nz, 4), P('istar', pv0 * npb, 4), None, m.nk, ng, nz,
+                                   m.dk, float(m.klims[0]), float(m.klims[1]), m.dg, tb['ze_ptr'],
+                                   P('ws'), g['wsb'], out_ptr, ldf, sp)
+                self._lib.check(st, "rr_ts_split")
+
+            if self.result == 'device':
+                launch(0, npv, self._lib.ptr(g['flux']))
+                ev = torch.cuda.Event()
+                ev.record(stream)
+                req.state['host_out'] = g['flux'][:, :, :npt]
+                req.state['ts_done_event'] = ev
+                return
+            chunk = g['chunk']
+            host = torch.empty((npv, npb, npt), dtype=torch.float32, pin_memory=True)
+            req.state['host_out'] = host
+            outs = [torch.empty((chunk, npb, ldf), dtype=torch.float32, device=self.device) for _ in range(2)]
+            for o in outs:
+                o.record_stream(self.copy_stream)
+            for j, pv0 in enumerate(range(0, npv, chunk)):
+                n = min(chunk, npv - pv0)
+                out = outs[j % 2]
+                if j >= 2:
+                    # the buffer's previous chunk must have left for the host
+                    stream.wait_event(req.state['chunk_ev'][j % 2])
+                launch(pv0, n, self._lib.ptr(out))
+                ev = torch.cuda.Event()
+                ev.record(stream)
+                self.copy_stream.wait_event(ev)
+                with torch.cuda.stream(self.copy_stream):
+                    host[pv0:pv0 + n].copy_(out[:n, :, :npt], non_blocking=True)
+                    cev = torch.cuda.Event()
+                    cev.record(self.copy_stream)
+                req.state.setdefault('chunk_ev', [None, None])[j % 2] = cev
+            req.state['ts_done_event'] = cev
 
     def start_copy(self, req):
         torch = self.torch
@@ -560,10 +742,16 @@ class GpuExecutor:
         return out if self.result == 'device' else out.numpy()
 
     def release(self, req):
+        """Called once the request's GPU work and copies have completed."""
         slot = req.state.pop('slot', None)
         if slot is not None:
             self.free_slots.append(slot)
-        req.state.pop('g', None)
+        g = req.state.pop('g', None)
+        if g is not None and 'block' in g:
+            self.arena.free(*g['block'])
 
     def shutdown(self):
+        """Wait for the GPU and give the arena back to the device."""
         self.torch.cuda.synchronize(self.device)
+        self.arena = None
+        self.torch.cuda.empty_cache()

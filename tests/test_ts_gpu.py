@@ -62,7 +62,8 @@ def test_ts_200_channels_vs_oracle(precision):
     assert max_err(got, want) <= TOL[precision]
 
 
-def test_ts_many_samples_chunked():
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_ts_many_samples_chunked(precision):
     """More than 32 supersamples: the sample loop runs in chunks of 32."""
     rng = np.random.default_rng(2)
     time = np.linspace(-0.15, 0.15, 300)
@@ -73,6 +74,33 @@ def test_ts_many_samples_chunked():
             np.zeros(npv), np.zeros(npv))
     ref = oracle.OracleRoadRunner('quadratic', ts=True)
     ref.set_data(time, nsamples=[45], exptimes=[0.03])
-    m = ts('fp64')
+    m = ts(precision)
     m.set_data(time, nsamples=[45], exptimes=[0.03])
-    assert max_err(m.evaluate(*args), ref.evaluate(*args)) <= 1e-9
+    assert max_err(m.evaluate(*args), ref.evaluate(*args)) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("ns,exptime", [(1, 0.0), (4, 2 / 1440), (10, 2 / 1440)])
+def test_ts_short_exposures_vs_oracle(precision, ns, exptime):
+    """Short exposures: each in-box point's samples fall on a few LD-table rows
+    (one point per lane), with slow and fast orbits mixed so that some points
+    span many rows (the warp-per-point path) in the same tiles."""
+    rng = np.random.default_rng(7 + ns)
+    T = 2459000.0
+    time = T + np.arange(2000) * (2 / 1440)
+    npv, npb = 24, 37
+    k = rng.uniform(0.09, 0.11, (npv, npb))
+    ldc = np.stack([rng.uniform(0.2, 0.5, (npv, npb)), rng.uniform(0.1, 0.3, (npv, npb))], -1)
+    t0 = T + 0.3 + rng.normal(0, 1e-3, npv)
+    p = np.where(np.arange(npv) % 3 == 0, rng.uniform(0.5, 0.8, npv), rng.uniform(1, 10, npv))
+    a = np.where(np.arange(npv) % 3 == 0, rng.uniform(15, 20, npv), rng.uniform(3, 12, npv))
+    inc = np.arccos(rng.uniform(0, 0.9, npv) / a)
+    e, w = np.zeros(npv), np.zeros(npv)
+    ref = oracle.OracleRoadRunner('quadratic', ts=True)
+    ref.set_data(time, nsamples=[ns], exptimes=[exptime])
+    want = ref.evaluate(k, ldc, t0, p, a, inc, e, w)
+    m = ts(precision)
+    m.set_data(time, nsamples=[ns], exptimes=[exptime])
+    got = m.evaluate(k, ldc, t0, p, a, inc, e, w)
+    assert np.sum(want < 1) > 20000
+    assert max_err(got, want) <= TOL[precision]
