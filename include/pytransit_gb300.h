@@ -158,6 +158,13 @@ int rr_prepare_split(double t_ref, double t_absmax, const double *k, int nkc, co
                      const float *basis, int nb);
 int rr_flux_split(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb, int ng,
                   double dg, const void *workspace, float *flux, int ldflux, void *stream);
+/* rr_flux_split for the parameter vectors [pv0, pv1) of a workspace prepared
+ * for npv: flux[pv1 - pv0, ldflux] holds those rows.  Lets a caller compute
+ * the flux in pv chunks and move each chunk to the host while the next one
+ * is computed. */
+int rr_flux_split_range(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb, int ng,
+                        double dg, const void *workspace, int pv0, int pv1, float *flux, int ldflux,
+                        void *stream);
 
 /* ---- transmission-spectroscopy model --------------------------------------- */
 

@@ -53,6 +53,7 @@ def _sig(L):
                                     _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _vp, _vp, _sz, _vp,
                                     _i, _vp, _i, _vp, _i])
     L.rr_flux_split.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _vp, _i, _vp]
+    L.rr_flux_split_range.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
     L.rr_ts_workspace_bytes.argtypes = [_i, _i, _i, _i]
     L.rr_ts_workspace_bytes.restype = _sz
     _ts_tail = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _d,

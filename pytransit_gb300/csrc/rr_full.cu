@@ -909,13 +909,24 @@ int rr_prepare_split(double t_ref, double t_absmax, const double* k, int nkc, co
 
 int rr_flux_split(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
                   double dg, const void* workspace, float* flux, int ldflux, void* stream) {
+  return rr_flux_split_range(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, 0, npv, flux, ldflux, stream);
+}
+
+int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
+                        double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
+                        void* stream) {
   if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || ldflux < npt) return RR_ERR_ARG;
-  if (npv == 0 || npt == 0) return RR_OK;
+  if (pv0 < 0 || pv1 > npv || pv0 > pv1) return RR_ERR_ARG;
+  if (pv1 == pv0 || npt == 0) return RR_OK;
   SplitTables t = carve_split(const_cast<void*>(workspace), npv, npb, nlc, ng);
   FluxSplitArgs fa{};
   fa.times_ff = reinterpret_cast<const float2*>(times_ff);
   fa.lcids = lcids;
-  fa.orb32 = t.orb; fa.lc32 = t.lc; fa.ldm = t.ldm;
+  // the range's records: the kernel indexes pv from 0 within the range
+  fa.orb32 = t.orb + (size_t)pv0 * ORB32;
+  fa.lc32 = t.lc + (size_t)pv0 * nlc * LC32;
+  fa.ldm = t.ldm + (size_t)pv0 * npb * ng;
+  npv = pv1 - pv0;
   fa.npt = npt; fa.npv = npv; fa.npb = npb; fa.nlc = nlc; fa.ng = ng; fa.ldflux = ldflux;
   fa.inv_dg = (float)(1.0 / dg); fa.flux = flux;
   // blocks per pv: enough for about 16 blocks per SM, each warp looping over tiles

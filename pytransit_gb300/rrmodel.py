@@ -20,6 +20,7 @@ or garbles its input:
 * k in the last table cell (ik + 1 == nk) uses the exact 2D weight table;
 * the LD-table index is clamped at g in [1 - 1e-7, 1].
 """
+import ctypes as C
 from typing import Callable, List, Tuple, Union
 from warnings import warn
 
@@ -327,6 +328,43 @@ class RoadRunnerModel(TransitModel):
         return out
 
     # ------------------------------------------------------------------
+    def _flux_to_host(self, dd, npt, npv, nlc, npb, ws, out2d, device, nchunks=8):
+        """Split-path flux into the pinned host rows out2d[npv, npt]: the pv
+        range in chunks through two device buffers, the flux of chunk c+1
+        computed on the current stream while chunk c is copied on a copy
+        stream.  Returns the first non-zero status."""
+        import torch
+        from . import _lib
+        L, P = _lib.lib(), _lib.ptr
+        bounds = np.linspace(0, npv, min(nchunks, npv) + 1).astype(int)
+        rows = int(np.diff(bounds).max())
+        key = (device, rows, npt)
+        if getattr(self, '_pipe', None) is None or self._pipe[0] != key:
+            self._pipe = (key, [torch.empty((rows, npt), dtype=torch.float32, device=device) for _ in range(2)],
+                          torch.cuda.Stream(device))
+        _, bufs, cs = self._pipe
+        comp = torch.cuda.current_stream(device)
+        sp = C.c_void_p(comp.cuda_stream)
+        copied = [None, None]
+        for c in range(len(bounds) - 1):
+            pv0, pv1 = int(bounds[c]), int(bounds[c + 1])
+            b = bufs[c % 2]
+            if copied[c % 2] is not None:
+                comp.wait_event(copied[c % 2])
+            st = L.rr_flux_split_range(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg,
+                                       P(ws), pv0, pv1, P(b), npt, sp)
+            if st != 0:
+                return st
+            done = torch.cuda.Event()
+            done.record(comp)
+            cs.wait_event(done)
+            with torch.cuda.stream(cs):
+                out2d[pv0:pv1].copy_(b[:pv1 - pv0], non_blocking=True)
+                copied[c % 2] = torch.cuda.Event()
+                copied[c % 2].record(cs)
+        comp.wait_stream(cs)
+        return 0
+
     def evaluate(self, k: Union[float, ndarray], ldc: Union[ndarray, List], t0: Union[float, ndarray],
                  p: Union[float, ndarray], a: Union[float, ndarray], i: Union[float, ndarray],
                  e: Union[float, ndarray] = 0.0, w: Union[float, ndarray] = 0.0, copy: bool = True,
@@ -338,7 +376,9 @@ class RoadRunnerModel(TransitModel):
         float64 numpy array; with copy=False the torch tensor on the GPU
         (float64, or float32 in the split precision).  ``out``: an optional
         [npv, npt] torch tensor (pinned host memory or device) that receives the
-        flux; it is filled, synchronised and returned."""
+        flux; it is filled, synchronised and returned.  In the split path a
+        contiguous pinned host float32 tensor is filled in parameter-vector
+        chunks, each copied to the host while the next one is computed."""
         import torch
         from . import _lib
         user_out = out
@@ -359,9 +399,14 @@ class RoadRunnerModel(TransitModel):
         npar = int(ldc_d.shape[2]) if ldc_d is not None else 0
         basis, nb = self._basis(device, npar, split) if ldc_d is not None else (None, 0)
         kmin, kmax = float(self.klims[0]), float(self.klims[1])
+        # A pinned host float32 buffer for the split path is filled in pv
+        # chunks: chunk c+1 is computed while chunk c is copied to the host.
+        pipe = (split and user_out is not None and user_out.device.type == 'cpu' and user_out.is_pinned()
+                and user_out.is_contiguous() and user_out.numel() == npv * npt and user_out.dtype == torch.float32
+                and npv >= 2)
         if split:
             ldf = (npt + 3) // 4 * 4
-            res = torch.empty((npv, ldf), dtype=torch.float32, device=device)
+            res = None if pipe else torch.empty((npv, ldf), dtype=torch.float32, device=device)
             nep = t0.shape[1]
             wsb = L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, self.ng)
             ws = self._workspace(wsb, device)
@@ -371,10 +416,12 @@ class RoadRunnerModel(TransitModel):
                                     P(dd['nsamples']), P(dd['exptimes']), P(ldp), P(istar), P(tb['W32']), self.nk,
                                     self.ng, nz, self.dk, kmin, kmax, P(tb['ze']), P(ws), ws.numel(), stream,
                                     self.ld_law or 0, P(ldc_d), npar, P(basis), nb)
-            if st == 0:
+            if st == 0 and pipe:
+                st = self._flux_to_host(dd, npt, npv, nlc, npb, ws, user_out.view(npv, npt), device)
+            elif st == 0:
                 st = L.rr_flux_split(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg,
                                      P(ws), P(res), ldf, stream)
-            res = res[:, :npt]
+            res = None if pipe else res[:, :npt]
         else:
             res = torch.empty((npv, npt), dtype=torch.float64, device=device)
             wsb = L.rr_full_f64_workspace_bytes(npv, npb, self.ng)
@@ -390,8 +437,9 @@ class RoadRunnerModel(TransitModel):
                                    P(res), npt, stream)
         _lib.check(st, "rr_full")
         if user_out is not None:
-            src = res if user_out.dtype == res.dtype else res.to(user_out.dtype)
-            user_out.view(npv, npt).copy_(src, non_blocking=True)
+            if not pipe:
+                src = res if user_out.dtype == res.dtype else res.to(user_out.dtype)
+                user_out.view(npv, npt).copy_(src, non_blocking=True)
             torch.cuda.current_stream(device).synchronize()
             return user_out
         res = res.squeeze()

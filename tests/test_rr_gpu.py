@@ -211,3 +211,30 @@ def test_device_output_and_copy_false():
     out = m.evaluate(np.array([[0.1], [0.11]]), [0.3, 0.1], [0.0, 0.0], [2.0, 2.1], 7.0, 1.55, copy=False)
     assert isinstance(out, torch.Tensor) and out.is_cuda and out.shape == (2, 100)
     assert out.dtype == torch.float32
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("npt", [1000, 1003])
+def test_pinned_host_output(precision, npt):
+    """out= a pinned host tensor: the split path computes it in pv chunks and
+    copies each chunk while the next is computed (also for npt not a multiple
+    of 4 and uneven chunks); same values as the device result, and a second
+    call overwrites every element."""
+    import torch
+    rng = np.random.default_rng(3)
+    T = 2459000.0
+    time = T + np.linspace(-0.3, 0.3, npt)
+    npv = 37
+    args = (rng.uniform(0.08, 0.12, (npv, 1)), [0.3, 0.1], T + rng.normal(0, 1e-3, (npv, 1)),
+            rng.uniform(1, 3, npv), rng.uniform(5, 9, npv), np.full(npv, 1.54), 0.0, 0.0)
+    m = rr(precision=precision)
+    m.set_data(time)
+    want = m.evaluate(*args, copy=False).cpu()
+    dt = torch.float32 if precision == 'split' else torch.float64
+    out = torch.full((npv, npt), -7.0, dtype=dt, pin_memory=True)
+    got = m.evaluate(*args, out=out)
+    assert got is out
+    assert torch.equal(out, want.to(dt))
+    out.fill_(-7.0)
+    m.evaluate(*args, out=out)
+    assert torch.equal(out, want.to(dt))
