@@ -526,14 +526,93 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
   for (int q = 0; q < SPLIT_PTS; ++q)
     if (inb >> q & 1u) single = single && (__float_as_int(LCR[lcv[q] * LC32 + LC_NS]) == 1);
   if (__all_sync(FULL, single)) {
+    // One sample per point.  A point whose planet disk is fully inside the
+    // star (area pi k^2) is finished in place; points on the limb (kite area,
+    // two atan2) are gathered into the warp's list and evaluated 32 at a time,
+    // so that the costly branch runs with full lanes.
+    unsigned limb = 0;
+    float zq[SPLIT_PTS];
+    if (tlc >= 0) {
+      // one light curve in the tile: its record in registers, the orbit
+      // polynomial from vector loads, z = r2 rsqrt(r2) (2 ulp)
+      const float k = RT[LC_K], gsc = RT[LC_INV1PK] * inv_dg, invis = RT[LC_INVIS];
+      const float* lda = ldm_pv + __float_as_int(RT[LC_PB]) * ng;
+      const float lim_out = 1.0f + k, lim_in = (k < 1.0f) ? 1.0f - k : -1.0f;
+      const float area_in = float(PI) * k * k * invis;
+      const float4 ca = *reinterpret_cast<const float4*>(orb);
+      const float4 cb = *reinterpret_cast<const float4*>(orb + 4);
+      const float2 cc = *reinterpret_cast<const float2*>(orb + 8);
+#pragma unroll
+      for (int q = 0; q < SPLIT_PTS; ++q) {
+        zq[q] = 0.0f;
+        if (!(inb >> q & 1u)) continue;
+        const float t = tcq[q];
+        const float x = fmaf(t, fmaf(t, fmaf(t, fmaf(t, cb.x, ca.w), ca.z), ca.y), ca.x);
+        const float y = fmaf(t, fmaf(t, fmaf(t, fmaf(t, cc.y, cc.x), cb.w), cb.z), cb.y);
+        const float r2 = fmaf(x, x, y * y);
+        const float z = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
+        zq[q] = z;
+        if (!(z < lim_out)) {
+          res[q] = 1.0f - 0.0f * invis;            // no overlap: 1 - 0 / istar (NaN with a NaN istar)
+        } else if (z <= lim_in) {
+          const float gg = z * gsc;
+          const int i = min(max((int)gg, 0), ng - 2);
+          const float fr = gg - (float)i;
+          const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
+          res[q] = 1.0f - fmaf(fr, l1 - l0, l0) * area_in;
+        } else {
+          limb |= 1u << q;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < SPLIT_PTS; ++q) {
+        zq[q] = 0.0f;
+        if (!(inb >> q & 1u)) continue;
+        const float* R = LCR + lcv[q] * LC32;
+        const float k = R[LC_K];
+        const float z = sep_c_f32(tcq[q], orb);
+        zq[q] = z;
+        if (!(z < 1.0f + k)) {                         // no overlap: 1 - 0 / istar (NaN with a NaN istar)
+          res[q] = 1.0f - 0.0f * R[LC_INVIS];
+          continue;
+        }
+        if (k < 1.0f && z <= 1.0f - k) {
+          const float gg = z * R[LC_INV1PK] * inv_dg;
+          int i = (int)gg;
+          i = min(max(i, 0), ng - 2);
+          const float fr = gg - (float)i;
+          const float* lda = ldm_pv + __float_as_int(R[LC_PB]) * ng;
+          const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
+          res[q] = 1.0f - fmaf(fr, l1 - l0, l0) * (float(PI) * k * k) * R[LC_INVIS];
+        } else {
+          limb |= 1u << q;
+        }
+      }
+    }
+    if (!__ballot_sync(FULL, limb != 0)) return;
+    int nl = 0;
+    int posq[SPLIT_PTS];
 #pragma unroll
     for (int q = 0; q < SPLIT_PTS; ++q) {
-      if (!(inb >> q & 1u)) continue;
-      const float* R = LCR + lcv[q] * LC32;
-      const float k = R[LC_K];
-      const float z = sep_c_f32(tcq[q], orb);
-      float d = 0.0f;
-      if (z < 1.0f + k) {
+      const bool in = limb >> q & 1u;
+      const unsigned m = __ballot_sync(FULL, in);
+      posq[q] = -1;
+      if (in) {
+        const int pos = nl + __popc(m & ((1u << lane) - 1u));
+        L.tc[pos] = zq[q];
+        L.lc[pos] = lcv[q];
+        posq[q] = pos;
+      }
+      nl += __popc(m);
+    }
+    __syncwarp();
+    for (int i0 = 0; i0 < nl; i0 += 32) {
+      const int it = i0 + lane;
+      if (it < nl) {
+        const float z = L.tc[it];
+        const float* R = LCR + L.lc[it] * LC32;
+        const float k = R[LC_K];
         const float gg = z * R[LC_INV1PK] * inv_dg;
         int i = (int)gg;
         i = min(max(i, 0), ng - 2);
@@ -541,10 +620,14 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
         const float* lda = ldm_pv + __float_as_int(R[LC_PB]) * ng;
         const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
         float kap;
-        d = fmaf(fr, l1 - l0, l0) * ccia_star<float>(k, z, kap);
+        L.acc[it] = fmaf(fr, l1 - l0, l0) * ccia_star<float>(k, z, kap);
       }
-      res[q] = 1.0f - d * R[LC_INVIS];
     }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < SPLIT_PTS; ++q)
+      if (posq[q] >= 0) res[q] = 1.0f - L.acc[posq[q]] * LCR[lcv[q] * LC32 + LC_INVIS];
+    __syncwarp();
     return;
   }
   int nitems = 0;
@@ -658,33 +741,52 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
   const float4* meta = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(A.times_ff) +
                                                        time_meta_offset(A.npt));
   WarpList& L = lists[warp];
-  for (int tile = t_first + warp; tile < t_end; tile += t_step) {
-    const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
-    const bool full4 = pt0 + SPLIT_PTS <= A.npt;
-    float res[SPLIT_PTS] = {1.0f, 1.0f, 1.0f, 1.0f};
-    if (!valid) {
-#pragma unroll
-      for (int q = 0; q < SPLIT_PTS; ++q) res[q] = __int_as_float(0x7fc00000);
-    } else {
-      // Tile cull: the tile's time range against the box copies around it.
-      // The rounding of t - d0 and of j p is covered by the error bound in
-      // the box (flo, fhi).
-      bool tile_out = false;
-      const float4 tm = __ldg(meta + tile);                 // tmin, tmax, lc
+  const unsigned FULL = 0xffffffffu;
+  for (int j0 = 0; t_first + warp + j0 * t_step < t_end; j0 += 32) {
+    // The cull test of the warp's next 32 tiles, one tile per lane: the
+    // tile's time range (from its summary) against the box copies around it,
+    // the rounding of t - d0 and of j p covered by the error bound in the box
+    // (flo, fhi).  A culled tile is then only a store of ones.
+    const int tl = t_first + warp + (j0 + lane) * t_step;
+    bool cull = false;
+    if (valid && !wide && tl < t_end) {
+      const float4 tm = __ldg(meta + tl);
       const int tlc = __float_as_int(tm.z);
-      if (!wide && tlc >= 0) {
+      if (tlc >= 0) {
         const float4 f = *reinterpret_cast<const float4*>(LCR + tlc * LC32);  // flo, fhi, d0h, d0l
         const float smin = tm.x - f.z, smax = tm.y - f.z;
-        const float j0 = ceilf((smin - f.y) * inv_p);
+        const float j0f = ceilf((smin - f.y) * inv_p);
         bool hit = false;
 #pragma unroll
         for (int dj = -1; dj <= 1; ++dj) {
-          const float jj = j0 + (float)dj;
+          const float jj = j0f + (float)dj;
           hit = hit || (fmaf(jj, p_hi, f.x) <= smax && fmaf(jj, p_hi, f.y) >= smin);
         }
-        tile_out = !hit;
+        cull = !hit;
       }
-      if (!tile_out) {
+    }
+    const unsigned cmask = __ballot_sync(FULL, cull);
+    for (int jt = 0; jt < 32; ++jt) {
+      const int tile = t_first + warp + (j0 + jt) * t_step;
+      if (tile >= t_end) break;
+      const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
+      const bool full4 = pt0 + SPLIT_PTS <= A.npt;
+      if (cmask >> jt & 1u) {
+        if (full4 && row_vec) {
+          __stcs(reinterpret_cast<float4*>(row + pt0), make_float4(1.0f, 1.0f, 1.0f, 1.0f));
+        } else {
+          for (int q = 0; q < SPLIT_PTS; ++q)
+            if (pt0 + q < A.npt) __stcs(row + pt0 + q, 1.0f);
+        }
+        continue;
+      }
+      float res[SPLIT_PTS] = {1.0f, 1.0f, 1.0f, 1.0f};
+      if (!valid) {
+#pragma unroll
+        for (int q = 0; q < SPLIT_PTS; ++q) res[q] = __int_as_float(0x7fc00000);
+      } else {
+        // the tile reaches a box copy (the cull test above said so)
+        const float4 tm = __ldg(meta + tile);                 // tmin, tmax, lc
         float hi[SPLIT_PTS], lo[SPLIT_PTS];
         int lcv[SPLIT_PTS];
         if (full4 && ((reinterpret_cast<uintptr_t>(A.times_ff + pt0) & 15) == 0) &&
@@ -709,12 +811,12 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
         }
         split_tile_points(orb, LCR, ldm_pv, A.ng, A.inv_dg, wide, tm, hi, lo, lcv, L, lane, res);
       }
-    }
-    if (full4 && row_vec) {
-      __stcs(reinterpret_cast<float4*>(row + pt0), make_float4(res[0], res[1], res[2], res[3]));
-    } else {
-      for (int q = 0; q < SPLIT_PTS; ++q)
-        if (pt0 + q < A.npt) __stcs(row + pt0 + q, res[q]);
+      if (full4 && row_vec) {
+        __stcs(reinterpret_cast<float4*>(row + pt0), make_float4(res[0], res[1], res[2], res[3]));
+      } else {
+        for (int q = 0; q < SPLIT_PTS; ++q)
+          if (pt0 + q < A.npt) __stcs(row + pt0 + q, res[q]);
+      }
     }
   }
 }
