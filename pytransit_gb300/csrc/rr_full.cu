@@ -542,24 +542,31 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
       const float4 ca = *reinterpret_cast<const float4*>(orb);
       const float4 cb = *reinterpret_cast<const float4*>(orb + 4);
       const float2 cc = *reinterpret_cast<const float2*>(orb + 8);
+      // the four points side by side, without branches until the loads are
+      // issued, so that their dependent chains overlap
+      float frq[SPLIT_PTS], l0q[SPLIT_PTS], l1q[SPLIT_PTS];
 #pragma unroll
       for (int q = 0; q < SPLIT_PTS; ++q) {
-        zq[q] = 0.0f;
-        if (!(inb >> q & 1u)) continue;
         const float t = tcq[q];
         const float x = fmaf(t, fmaf(t, fmaf(t, fmaf(t, cb.x, ca.w), ca.z), ca.y), ca.x);
         const float y = fmaf(t, fmaf(t, fmaf(t, fmaf(t, cc.y, cc.x), cb.w), cb.z), cb.y);
         const float r2 = fmaf(x, x, y * y);
-        const float z = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
-        zq[q] = z;
-        if (!(z < lim_out)) {
+        zq[q] = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
+        const float gg = fminf(zq[q], lim_out) * gsc;
+        const int i = min(max((int)gg, 0), ng - 2);
+        frq[q] = gg - (float)i;
+        const bool need = (inb >> q & 1u) && zq[q] <= lim_in;
+        l0q[q] = need ? __ldg(lda + i) : 0.0f;
+        l1q[q] = need ? __ldg(lda + i + 1) : 0.0f;
+      }
+#pragma unroll
+      for (int q = 0; q < SPLIT_PTS; ++q) {
+        if (!(inb >> q & 1u)) {
+          zq[q] = 0.0f;
+        } else if (!(zq[q] < lim_out)) {
           res[q] = 1.0f - 0.0f * invis;            // no overlap: 1 - 0 / istar (NaN with a NaN istar)
-        } else if (z <= lim_in) {
-          const float gg = z * gsc;
-          const int i = min(max((int)gg, 0), ng - 2);
-          const float fr = gg - (float)i;
-          const float l0 = __ldg(lda + i), l1 = __ldg(lda + i + 1);
-          res[q] = 1.0f - fmaf(fr, l1 - l0, l0) * area_in;
+        } else if (zq[q] <= lim_in) {
+          res[q] = 1.0f - fmaf(frq[q], l1q[q] - l0q[q], l0q[q]) * area_in;
         } else {
           limb |= 1u << q;
         }
