@@ -569,6 +569,20 @@ def main():
     torch.cuda.synchronize(device)
     dF = float((flux32[:, :npt].double() - flux64).abs().max().item())
     in_transit = float((flux64 < 1.0).double().mean().item())
+    # independent cross-check: the Mandel & Agol quadratic model on the same
+    # orbit layer as the FP64 RoadRunner step just run (its workspace)
+    ma_check = None
+    if not args.no_extra:
+        from pytransit_gb300 import crosscheck
+        fma = torch.empty_like(flux64)
+        _lib.check(crosscheck._L().rr_ma_quad_flux_f64(
+            P(dd["time"]), npt, P(dev["k"]), 1, P(dev["t0"]), 1, P(dev["p"]), npv, nlc, npb, P(dd["lcids"]),
+            P(dd["pbids"]), P(dd["epids"]), P(dd["nsamples"]), P(dd["exptimes"]), P(dev["ldc"]), P(ws64), P(fma),
+            npt, sp), "rr_ma_quad_flux_f64")
+        ma_check = {"max_abs_dF_roadrunner_vs_mandel_agol": float((flux64 - fma).abs().max().item()),
+                    "what": "plain FP64 RoadRunner vs the Mandel & Agol quadratic model (elliptic integrals) on "
+                            "the same orbit, fold and bounding box, whole workload: RoadRunner's discretisation"}
+        del fma
 
     # --- end to end through the public API: host params in, pinned host flux out ---
     host_out = torch.empty((npv, npt), dtype=torch.float32, pin_memory=True)
@@ -614,6 +628,7 @@ def main():
         "fp64_path": {"value": value64, "unit": "model points/s", "ms_per_step": ms64 / fp64_steps},
         "split_over_fp64": value / value64,
         "max_abs_dF_vs_fp64": dF,
+        "mandel_agol_crosscheck": ma_check,
         "in_transit_fraction": in_transit,
         "e2e": {"value": e2e_value, "unit": "model points/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,

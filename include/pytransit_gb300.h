@@ -224,6 +224,25 @@ int rr_lnlike_split(int law, const double *ldc, int npar, const double *mu, cons
                     double kmax, double dg, const double *z_edges, const double *obs, const double *sigma,
                     void *workspace, size_t workspace_bytes, double *lnl, double *grad, void *stream);
 
+/* ---- independent cross-check: the Mandel & Agol quadratic model ----------- */
+
+/* Flux of a star with quadratic limb darkening (u1, u2) occulted by a disk of
+ * radius ratio k at the centre distances z[n], FP64: eval_quad_z_s
+ * (pytransit/models/numba/ma_quadratic_nb.py:277-389; Mandel & Agol 2002,
+ * complete elliptic integrals by Abramowitz & Stegun 17.3.34/36 and Bulirsch's
+ * iteration for the third kind). */
+int rr_ma_quad_z_f64(const double *z, int n, double k, double u1, double u2, double *flux, void *stream);
+/* The quadratic model on the RoadRunner orbit layer: with a workspace from
+ * rr_prepare_f64 (Taylor coefficients, contact points) and the arguments of
+ * rr_flux_f64, the same phase fold, z and bounding box, but the Mandel & Agol
+ * flux per sample (quadratic_model_v, ma_quadratic_nb.py:532-597) with
+ * ldc[npv, npb, 2].  Point by point against rr_flux_f64 this isolates the
+ * RoadRunner discretisation (weight tables, interpolation). */
+int rr_ma_quad_flux_f64(const double *times, int npt, const double *k, int nkc, const double *t0, int ldt0,
+                        const double *p, int npv, int nlc, int npb, const int32_t *lcids, const int32_t *pbids,
+                        const int32_t *epids, const int32_t *nsamples, const double *exptimes, const double *ldc,
+                        const void *workspace, double *flux, int ldflux, void *stream);
+
 /* ---- serving: many requests in one persistent launch ---------------------- */
 
 /* One request of the serving loop (all pointers on the device): the data of

@@ -77,6 +77,14 @@ def lib():
                                    C.c_double, C.c_double, C.c_double, C.c_double, _d, _d, C.c_int])
         L.rro_ts_full.restype = C.c_int
         L.rro_lnlike_normal.argtypes = [_d, _d, C.c_int, C.c_int, C.c_double, _d]
+        for n in ("rro_ellk", "rro_ellec"):
+            getattr(L, n).argtypes = [C.c_double]
+            getattr(L, n).restype = C.c_double
+        L.rro_ellpicb.argtypes = [C.c_double, C.c_double]
+        L.rro_ellpicb.restype = C.c_double
+        L.rro_ma_quad_z.argtypes = [C.c_double] * 4
+        L.rro_ma_quad_z.restype = C.c_double
+        L.rro_ma_quad_z_v.argtypes = [_d, C.c_int, C.c_double, C.c_double, C.c_double, _d]
         _LIB = L
     return _LIB
 
@@ -236,6 +244,15 @@ def ts_full(times, k, t0, p, a, i, e, w, nsamples0, exptime0, ldp, istar, weight
                       npv, npb, int(nsamples0), float(exptime0), _dp(ldp), _dp(istar), wp, nk, ng, nz,
                       dk or 0.0, kmin, kmax, dg or 0.0, _dp(z_edges), _dp(flux), nthreads)
     return flux
+
+
+def ma_quad_z(z, k, u1, u2):
+    """Mandel & Agol quadratic-LD flux at centre distances z (eval_quad_z_s,
+    pytransit/models/numba/ma_quadratic_nb.py:277-389)."""
+    z = _f64(np.atleast_1d(z))
+    out = np.empty_like(z)
+    lib().rro_ma_quad_z_v(_dp(z), z.size, float(k), float(u1), float(u2), _dp(out))
+    return out
 
 
 def lnlike_normal(obs, model, sigma):

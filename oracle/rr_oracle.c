@@ -643,3 +643,131 @@ void rro_lnlike_normal(const double *obs, const double *model, int npv, int npt,
         lnl[ipv] = -npt * log(sigma) - 0.5 * npt * log(2 * RRO_PI) - 0.5 * s;
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* Mandel & Agol (2002) quadratic model, the independent cross-check:  */
+/* eval_quad_z_s, pytransit/models/numba/ma_quadratic_nb.py:277-389     */
+/* ------------------------------------------------------------------ */
+
+/* Complete elliptic integral of the first kind, K(k), by the polynomial
+ * approximation of Abramowitz & Stegun 17.3.34 in m1 = 1 - k^2
+ * (ellk, ma_quadratic_nb.py:110-126). */
+double rro_ellk(double k)
+{
+    double m1 = 1.0 - k * k;
+    double ek1 = 1.386294361120 + m1 * (0.096663442590 + m1 * (0.035900923830 + m1 * (0.037425637130 +
+                 m1 * 0.014511962120)));
+    double ek2 = (0.50 + m1 * (0.124985935970 + m1 * (0.068802485760 + m1 * (0.033283553460 +
+                 m1 * 0.004417870120)))) * log(m1);
+    return ek1 - ek2;
+}
+
+/* Complete elliptic integral of the second kind, E(k), Abramowitz & Stegun
+ * 17.3.36 (ellec, ma_quadratic_nb.py:93-107). */
+double rro_ellec(double k)
+{
+    double m1 = 1.0 - k * k;
+    double ee1 = 1.0 + m1 * (0.443251414630 + m1 * (0.062606012200 + m1 * (0.047573835460 +
+                 m1 * 0.017365064510)));
+    double ee2 = m1 * (0.249983683100 + m1 * (0.092001800370 + m1 * (0.040696975260 +
+                 m1 * 0.005264496390))) * log(1.0 / m1);
+    return ee1 + ee2;
+}
+
+/* Complete elliptic integral of the third kind, Pi(n, k), by Bulirsch's
+ * (1965) iteration (ellpicb, ma_quadratic_nb.py:55-90); 0 when it does not
+ * converge in 1000 steps. */
+double rro_ellpicb(double n, double k)
+{
+    double kc = sqrt(1.0 - k * k), e = kc, p = sqrt(n + 1.0), m0 = 1.0, c = 1.0, d = 1.0 / p;
+    for (int it = 0; it < 1000; ++it) {
+        double f = c;
+        c = d / p + c;
+        double g = e / p;
+        d = 2.0 * (f * g + d);
+        p = g + p;
+        g = m0;
+        m0 = kc + m0;
+        if (fabs(1.0 - kc / g) > 1e-8) {
+            kc = 2.0 * sqrt(e);
+            e = kc * m0;
+        } else {
+            return 0.5 * RRO_PI * (c * m0 + d) / (m0 * (m0 + p));
+        }
+    }
+    return 0.0;
+}
+
+/* Flux of a star with quadratic limb darkening (u1, u2) occulted by a disk
+ * of radius k at centre distance z (Mandel & Agol 2002, Tables 1 and 3), as
+ * eval_quad_z_s computes it:
+ *   k within 1e-4 of 1/2 is set to 1/2, z within 1e-6 of k is moved by +1e-6;
+ *   z > 1 + k or z of negative sign -> 1; k >= 1 and z <= k - 1 -> 0;
+ *   the limb angles kap0, kap1 exist only in the ingress/egress branch of
+ *   the uniform term; where a later branch reads them without it (z = 1 - k
+ *   exactly) they are 0, the value the reference's compiled code uses
+ *   (its own test pins F(1 - k) = 0.99164875 for k = 0.1, u = (0.2, 0.1)). */
+double rro_ma_quad_z(double z, double k, double u1, double u2)
+{
+    const double inv_pi = 1.0 / RRO_PI;
+    if (fabs(k - 0.5) < 1.0e-4) k = 0.5;
+    double k2 = k * k;
+    double omega = 1.0 - u1 / 3.0 - u2 / 6.0;
+    if (fabs(z - k) < 1e-6) z += 1e-6;
+    if (z > 1.0 + k || signbit(z)) return 1.0;
+    if (k >= 1.0 && z <= k - 1.0) return 0.0;
+    double z2 = z * z, x1 = (k - z) * (k - z), x2 = (k + z) * (k + z), x3 = k * k - z * z;
+    double le = 0.0, ld = 0.0, ed = 0.0, kap0 = 0.0, kap1 = 0.0;
+    if (z <= 1.0 - k) {
+        le = k2;
+    } else if (z >= fabs(1.0 - k) && z <= 1.0 + k) {
+        kap1 = acos(fmin((1.0 - k2 + z2) / (2.0 * z), 1.0));
+        kap0 = acos(fmin((k2 + z2 - 1.0) / (2.0 * k * z), 1.0));
+        le = k2 * kap0 + kap1;
+        le = (le - 0.5 * sqrt(fmax(4.0 * z2 - (1.0 + z2 - k2) * (1.0 + z2 - k2), 0.0))) * inv_pi;
+    }
+    int edge_at_origin = fabs(z - k) < 1.e-4 * (z + k);
+    int full_transit = k <= 1.0 && z < (1.0 - k);
+    if (edge_at_origin) {
+        if (k == 0.5) {
+            ld = 1.0 / 3.0 - 4.0 * inv_pi / 9.0;
+            ed = 3.0 / 32.0;
+        } else if (z > 0.5) {
+            double q = 0.5 / k, Kk = rro_ellk(q), Ek = rro_ellec(q);
+            ld = 1.0 / 3.0 + 16.0 * k / 9.0 * inv_pi * (2.0 * k2 - 1.0) * Ek -
+                 (32.0 * k2 * k2 - 20.0 * k2 + 3.0) / 9.0 * inv_pi / k * Kk;
+            ed = 0.5 * inv_pi * (kap1 + k2 * (k2 + 2.0 * z2) * kap0 -
+                                 (1.0 + 5.0 * k2 + z2) / 4.0 * sqrt((1.0 - x1) * (x2 - 1.0)));
+        } else if (z < 0.5) {
+            double q = 2.0 * k, Kk = rro_ellk(q), Ek = rro_ellec(q);
+            ld = 1.0 / 3.0 + 2.0 / 9.0 * inv_pi * (4.0 * (2.0 * k2 - 1.0) * Ek + (1.0 - 4.0 * k2) * Kk);
+            ed = k2 / 2.0 * (k2 + 2.0 * z2);
+        }
+    } else if (full_transit) {
+        double q = sqrt((x2 - x1) / (1.0 - x1)), Kk = rro_ellk(q), Ek = rro_ellec(q);
+        double Pk = rro_ellpicb(x2 / x1 - 1.0, q);
+        ld = 2.0 / 9.0 * inv_pi / sqrt(1.0 - x1) *
+             ((1.0 - 5.0 * z2 + k2 + x3 * x3) * Kk + (1.0 - x1) * (z2 + 7.0 * k2 - 4.0) * Ek - 3.0 * x3 / x1 * Pk);
+        if (z < k) ld = ld + 2.0 / 3.0;
+        if (fabs(k + z - 1.0) < 1.e-4)
+            ld = 2.0 / 3.0 * inv_pi * acos(1.0 - 2.0 * k) - 4.0 / 9.0 * inv_pi * sqrt(k * (1.0 - k)) *
+                 (3.0 + 2.0 * k - 8.0 * k2);
+        ed = k2 / 2.0 * (k2 + 2.0 * z2);
+    } else {
+        double q = sqrt((1.0 - (k - z) * (k - z)) / 4.0 / z / k), Kk = rro_ellk(q), Ek = rro_ellec(q);
+        double Pk = rro_ellpicb(1.0 / x1 - 1.0, q);
+        ld = 1.0 / 9.0 * inv_pi / sqrt(k * z) *
+             (((1.0 - x2) * (2.0 * x2 + x1 - 3.0) - 3.0 * x3 * (x2 - 2.0)) * Kk +
+              4.0 * k * z * (z2 + 7.0 * k2 - 4.0) * Ek - 3.0 * x3 / x1 * Pk);
+        if (z < k) ld = ld + 2.0 / 3.0;
+        ed = 0.5 * inv_pi * (kap1 + k2 * (k2 + 2.0 * z2) * kap0 -
+                             (1.0 + 5.0 * k2 + z2) / 4.0 * sqrt((1.0 - x1) * (x2 - 1.0)));
+    }
+    return 1.0 - ((1.0 - u1 - 2.0 * u2) * le + (u1 + 2.0 * u2) * ld + u2 * ed) / omega;
+}
+
+/* rro_ma_quad_z over an array of z. */
+void rro_ma_quad_z_v(const double *z, int n, double k, double u1, double u2, double *flux)
+{
+    for (int i = 0; i < n; ++i) flux[i] = rro_ma_quad_z(z[i], k, u1, u2);
+}

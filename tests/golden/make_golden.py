@@ -17,8 +17,9 @@ Everything except the orbit layer is therefore the reference's own code:
 RoadRunnerModel.__init__/set_data/evaluate (rrmodel.py), rr_full and rr_simple
 (model_full.py, model_simple.py), the weight tables, area and interpolation
 (common.py), the LD laws (numba/ldmodels.py), LDModel (ldmodel.py),
-TransitModel.set_data (transitmodel.py) and TransmissionSpectroscopyModel /
-tsmodel_serial (tsmodel.py, model_trspec.py).
+TransitModel.set_data (transitmodel.py), TransmissionSpectroscopyModel /
+tsmodel_serial (tsmodel.py, model_trspec.py) and the Mandel & Agol quadratic
+model used as the independent cross-check (numba/ma_quadratic_nb.py).
 """
 import os
 import sys
@@ -285,8 +286,37 @@ def case_tables():
          dg2=dg2, w2=W2, lda=lda, gs=gs, interp=interp)
 
 
+def case_ma_quadratic():
+    """The reference's Mandel & Agol quadratic model, eval_quad_z_s
+    (pytransit/models/numba/ma_quadratic_nb.py), over z grids for several k
+    and limb darkening coefficients, with the special points (z = 0, k, 1,
+    1 + k, near 1 - k and the k = 1/2 edge case).  Points where the pure-Python
+    function fails (exactly z = 1 - k reads the unassigned limb angles) are
+    left out (ok = False).  Some z give NaN in the reference (a negative
+    square root near the limb); those are kept."""
+    from pytransit.models.numba.ma_quadratic_nb import eval_quad_z_s
+    rng = np.random.default_rng(29)
+    ks = np.array([0.01, 0.05, 0.1, 0.12, 0.3, 0.5, 0.50005, 0.7, 1.2])
+    us = np.array([[0.0, 0.0], [0.2, 0.1], [0.6, 0.3], [0.1, 0.5]])
+    zs = np.concatenate([np.linspace(0.0, 2.3, 600), rng.uniform(0.0, 2.3, 200)])
+    flux = np.full((ks.size, us.shape[0], zs.size + 8), np.nan)
+    ok = np.zeros(flux.shape, bool)
+    zall = np.zeros((ks.size, zs.size + 8))
+    for ik, k in enumerate(ks):
+        zk = np.concatenate([zs, [0.0, k, 1.0, 1.0 + k, 1.0 - k + 1e-7, 1.0 - k - 1e-7, k + 5e-7, 0.5]])
+        zall[ik] = zk
+        for iu, u in enumerate(us):
+            for iz, z in enumerate(zk):
+                try:
+                    flux[ik, iu, iz] = eval_quad_z_s(z, k, u)
+                    ok[ik, iu, iz] = True
+                except UnboundLocalError:
+                    pass
+    save("ma_quadratic", ks=ks, us=us, z=zall, flux=flux, ok=ok)
+
+
 if __name__ == "__main__":
     for f in (case_tables, case_c0, case_multi, case_power2, case_laws, case_user_ld, case_klims,
-              case_simple, case_ts):
+              case_simple, case_ts, case_ma_quadratic):
         print(f.__name__)
         f()

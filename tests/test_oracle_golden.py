@@ -186,3 +186,31 @@ def test_mandel_agol_cross_check():
         a, _ = oracle.ccia(1.0, k, z)
         f = (istar[0, 0] - ip * a) / istar[0, 0]
         assert abs(f - want) <= tol, (z, f, want)
+
+
+# --- Mandel & Agol quadratic model (the independent cross-check) -----------
+
+def test_ma_quadratic_known_answers():
+    """The reference's own pins of eval_quad_z_s (tests/test_ma_quadratic_nb.py):
+    k = 0.1, u = (0, 0) and (0.2, 0.1), including z = 1 - k, and radius ratios >= 1."""
+    K, L0, L1 = 0.1, (0.0, 0.0), (0.2, 0.1)
+    pins = [(-2.0, L1, 1.0), (2.0, L1, 1.0), (0.2, L0, 1 - K * K), (0.2, L1, 0.98914137),
+            (-0.0, L1, 1.0), (0.0, L0, 1 - K * K), (0.0, L1, 0.98909638), (K, L0, 1 - K * K),
+            (K, L1, 0.98910745), (1 - K, L0, 1 - K * K), (1 - K, L1, 0.99164875), (1.0, L0, 0.99510612),
+            (1.0, L1, 0.99573423), (1 + K, L0, 1.0), (1 + K, L1, 1.0)]
+    for z, u, want in pins:
+        np.testing.assert_almost_equal(oracle.ma_quad_z(z, K, *u)[0], want)
+    for z, k, want in [(-0.0, 1.0, 1.0), (0.0, 1.0, 0.0), (0.0, 1.1, 0.0), (1.0, 2.0, 0.0)]:
+        np.testing.assert_almost_equal(oracle.ma_quad_z(z, k, *L1)[0], want)
+
+
+def test_ma_quadratic_matches_reference(golden):
+    g = golden("ma_quadratic")
+    for ik, k in enumerate(g["ks"]):
+        for iu, u in enumerate(g["us"]):
+            ok = g["ok"][ik, iu]
+            want = g["flux"][ik, iu][ok]
+            got = oracle.ma_quad_z(g["z"][ik], k, *u)[ok]
+            assert np.array_equal(np.isnan(got), np.isnan(want)), (k, u)
+            m = ~np.isnan(want)
+            assert np.abs(got[m] - want[m]).max() <= 1e-12, (k, u)

@@ -13,12 +13,15 @@ from pytransit_gb300.serving import RRServer, request_bytes, shape_request, work
 class FakeExecutor:
     """Completes a request one step after its last items were issued."""
 
-    def __init__(self):
+    def __init__(self, setup_delay=0.0):
         self.log = []
         self.lock = threading.Lock()
         self.max_inflight_bytes = 0
+        self.setup_delay = setup_delay
 
     def setup(self, req, ts_chunk_bytes):
+        if self.setup_delay:
+            time.sleep(self.setup_delay)     # the other requests are queued meanwhile
         self.log.append(('setup', req.rid))
 
     def step(self, batch, ts):
@@ -78,7 +81,7 @@ def test_admission_by_budget_and_completion():
 
 
 def test_requests_share_steps_round_robin():
-    ex = FakeExecutor()
+    ex = FakeExecutor(setup_delay=0.05)
     srv = RRServer(executor=ex, hbm_budget=1e12, step_items=6)
     futs = [srv.submit('rr', 'quadratic', *rr_req(40, 128 * 10)) for _ in range(3)]
     [f.result(timeout=10) for f in futs]
