@@ -243,6 +243,16 @@ int rr_ma_quad_flux_f64(const double *times, int npt, const double *k, int nkc, 
                         const int32_t *epids, const int32_t *nsamples, const double *exptimes, const double *ldc,
                         const void *workspace, double *flux, int ldflux, void *stream);
 
+/* ---- sampler parameter mapping -------------------------------------------- */
+
+/* BaseLPF.transit_model's parameter mapping (pytransit/lpf/lpf.py:435-443) on
+ * the device: pv[npv, ldpv] rows [tc, p, rho, b, k2, q1, q2 per passband from
+ * column ld_start] -> k = sqrt(k2), t0 = tc - tref, p, a = as_from_rhop(rho, p)
+ * (pytransit/orbits/orbits_py.py:604-618), i = i_from_ba(b, a)
+ * (orbits_py.py:674-689), ldc[npv, npb, 2] = map_ldc(q) (lpf.py:85-91). */
+int rr_lpf_map(const double *pv, int npv, int ldpv, int npb, int ld_start, double tref, double *k, double *t0,
+               double *p, double *a, double *inc, double *ldc, void *stream);
+
 /* ---- serving: many requests in one persistent launch ---------------------- */
 
 /* One request of the serving loop (all pointers on the device): the data of

@@ -379,17 +379,25 @@ class RoadRunnerModel(TransitModel):
         flux; it is filled, synchronised and returned.  In the split path a
         contiguous pinned host float32 tensor is filled in parameter-vector
         chunks, each copied to the host while the next one is computed."""
+        device = self._cuda_device()
+        k, t0, p, a, i, e, w = self._shape_params(k, t0, p, a, i, e, w)
+        ldc3 = self._shape_ldc(ldc, p.size, self.npb) if self.ld_law is not None else None
+        args = self._upload(dict(k=k, t0=t0, p=p, a=a, i=i, e=e, w=w, ldc=ldc3), device)
+        return self._evaluate_device(args, ldc, out, copy)
+
+    def _evaluate_device(self, args, ldc=None, out=None, copy=False):
+        """The device half of evaluate: args holds float64 device tensors k[npv,
+        nkc], t0[npv, nep], p, a, i, e, w[npv] and, for a named law, ldc[npv, npb,
+        ncoef] (ldc: the host coefficients, used only by host LD models)."""
         import torch
         from . import _lib
         user_out = out
         device = self._cuda_device()
-        k, t0, p, a, i, e, w = self._shape_params(k, t0, p, a, i, e, w)
-        npv, npt, npb, nlc = p.size, self.npt, self.npb, self.nlc
+        k, t0 = args['k'], args['t0']
+        npv, npt, npb, nlc = args['p'].numel(), self.npt, self.npb, self.nlc
         split = self.precision == 'split'
         tb = self._device_tables(device)
         dd = self._device_data(device)
-        ldc3 = self._shape_ldc(ldc, npv, npb) if self.ld_law is not None else None
-        args = self._upload(dict(k=k, t0=t0, p=p, a=a, i=i, e=e, w=w, ldc=ldc3), device)
         ldp, istar = self._ld_tables(ldc, npv, npb, device, split, args.get('ldc'))
         L = _lib.lib()
         stream = _lib.stream_ptr(device)

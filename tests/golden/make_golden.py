@@ -315,8 +315,32 @@ def case_ma_quadratic():
     save("ma_quadratic", ks=ks, us=us, z=zall, flux=flux, ok=ok)
 
 
+def case_lpf_map():
+    """BaseLPF.transit_model's parameter mapping from the reference's own code:
+    as_from_rhop and i_from_ba (pytransit/orbits/orbits_py.py) imported, and
+    map_ldc (pytransit/lpf/lpf.py:85-91) taken from the source file and
+    executed on its own (lpf.py's module imports - xarray, arviz, astropy,
+    matplotlib - are not installed here)."""
+    import ast
+    from pytransit.orbits.orbits_py import as_from_rhop, i_from_ba
+    src = open(os.path.join(REF, "pytransit", "lpf", "lpf.py")).read()
+    fn = next(n for n in ast.parse(src).body if isinstance(n, ast.FunctionDef) and n.name == "map_ldc")
+    fn.decorator_list = []
+    ns = {"atleast_2d": np.atleast_2d, "zeros_like": np.zeros_like, "sqrt": np.sqrt}
+    exec(compile(ast.Module(body=[fn], type_ignores=[]), "lpf.py", "exec"), ns)
+    map_ldc = ns["map_ldc"]
+    rng = np.random.default_rng(37)
+    npv, npb, tref = 500, 3, 2459000.0
+    pv = np.column_stack([tref + rng.normal(0.3, 0.01, npv), rng.uniform(0.5, 20, npv), rng.uniform(0.1, 25, npv),
+                          rng.uniform(0, 1, npv), rng.uniform(0.0025, 0.04, npv)] +
+                         [rng.uniform(0, 1, npv) for _ in range(2 * npb)])
+    a = as_from_rhop(pv[:, 2], pv[:, 1])
+    save("lpf_map", pv=pv, tref=tref, npb=npb, k=np.sqrt(pv[:, 4:5]), t0=pv[:, 0] - tref, p=pv[:, 1], a=a,
+         inc=i_from_ba(pv[:, 3], a), ldc=map_ldc(pv[:, 5:]).reshape(npv, npb, 2))
+
+
 if __name__ == "__main__":
     for f in (case_tables, case_c0, case_multi, case_power2, case_laws, case_user_ld, case_klims,
-              case_simple, case_ts, case_ma_quadratic):
+              case_simple, case_ts, case_ma_quadratic, case_lpf_map):
         print(f.__name__)
         f()
