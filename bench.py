@@ -131,8 +131,10 @@ class ClockSampler:
         smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[j] for r in rows for j in range(4) if r[4 + j].lower() == "active"})
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "sm_mhz_min": min(sm) if sm else None,
+                "power_w_max": max(pw) if pw else None}
 
 
 def cpu_rr_full(model, prm, npv_sample, nthreads):
@@ -357,6 +359,7 @@ def bench_serve(args):
     srv.submit(*c4_requests(2, seed=99)[0], keep_result=False).result()
     done_t = {}
     futs = []
+    clk = ClockSampler(0).__enter__()
     t_start = time.perf_counter()
     t_next = t_start
     for j, (r, gap) in enumerate(zip(reqs, gaps)):
@@ -377,6 +380,8 @@ def bench_serve(args):
             rejected.add(j)
         futs[j] = None
     t_end = time.perf_counter()
+    clk.__exit__(None, None, None)
+    clocks = clk.summary()
     stats = srv.stats.summary()
     srv.close()
     # the same requests one at a time through the drop-in models (no batching):
@@ -422,6 +427,7 @@ def bench_serve(args):
             "wall_s": t_end - t_start, "offered_req_per_s": args.rate,
             "achieved_req_per_s": stats["completed"] / (t_end - t_start),
             "peak_admitted_bytes": stats["peak_hbm_bytes"],
+            "clocks": clocks,
             "plain_fp64_per_request": dict(per_req["fp64"], sample="the same requests one at a time (data upload "
                                            "included), RoadRunnerModel / TransmissionSpectroscopyModel "
                                            "precision='fp64', copy=False"),

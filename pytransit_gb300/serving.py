@@ -26,6 +26,7 @@ exercised on the CPU with a fake executor (tests/test_serving_cpu.py).
 import bisect
 import collections
 import concurrent.futures as cf
+import gc
 import ctypes as C
 import itertools
 import threading
@@ -214,23 +215,35 @@ class _PinnedRing:
         self.live.append((lo, lo + ((n + 255) & ~255), event))
 
 
-def work_items(npv: int, npt: int, target_tiles: int = 256):
-    """(pv0, pv1, tile0, tile1) chunks of about target_tiles pv-tiles each."""
+def work_items(npv: int, npt: int, target_tiles: int = 256) -> np.ndarray:
+    """Rows (pv0, pv1, tile0, tile1) of about target_tiles pv-tiles each (int32)."""
     ntiles = max(1, (npt + TILE - 1) // TILE)
     if ntiles >= target_tiles:
-        return [(pv, pv + 1, t, min(t + target_tiles, ntiles)) for pv in range(npv)
-                for t in range(0, ntiles, target_tiles)]
+        t0 = np.arange(0, ntiles, target_tiles)
+        pv = np.repeat(np.arange(npv), t0.size)
+        tt = np.tile(t0, npv)
+        return np.stack([pv, pv + 1, tt, np.minimum(tt + target_tiles, ntiles)], 1).astype(np.int32)
     per = max(1, target_tiles // ntiles)
-    return [(pv, min(pv + per, npv), 0, ntiles) for pv in range(0, npv, per)]
+    pv0 = np.arange(0, npv, per)
+    return np.stack([pv0, np.minimum(pv0 + per, npv), np.zeros_like(pv0), np.full_like(pv0, ntiles)],
+                    1).astype(np.int32)
 
 
 class RRServer:
     """Continuous-batching server (see the module docstring)."""
 
     def __init__(self, executor=None, hbm_budget: float = 120e9, step_items: int = 4096,
-                 ts_chunk_bytes: float = 4e9, device=None, result: str = 'host'):
+                 ts_chunk_bytes: float = 4e9, device=None, result: str = 'host', freeze_gc: bool = True):
+        """freeze_gc: move every object that exists when the server starts (the
+        imported modules of torch, numpy, ...) out of the cyclic garbage
+        collector's generations (gc.freeze), so that a full collection during
+        serving scans only the objects made since, not pausing every thread
+        for tens of milliseconds."""
         self.ex = executor if executor is not None else GpuExecutor(
             device, result=result, arena_bytes=int(hbm_budget * 1.1) + (1 << 30))
+        if freeze_gc:
+            gc.collect()
+            gc.freeze()
         self.budget = int(hbm_budget)
         self.step_items = step_items
         self.ts_chunk_bytes = ts_chunk_bytes
@@ -329,7 +342,8 @@ class RRServer:
                     self._queue.appendleft(req)
                 return
             if req.kind == 'rr':
-                req.state['items'] = collections.deque(work_items(req.npv, req.npt))
+                req.state['items'] = work_items(req.npv, req.npt)
+                req.state['icur'] = 0
             else:
                 self._ts_new.append(req)
             with self._cv:
@@ -337,19 +351,22 @@ class RRServer:
                 self.stats.admitted += 1
 
     def _take_items(self):
-        """Round-robin over active plain requests, up to step_items items."""
-        batch = []
-        rr = [r for r in self._active.values() if r.kind == 'rr' and r.state.get('items')]
-        while rr and len(batch) < self.step_items:
+        """Round-robin over active plain requests, up to step_items work items:
+        a list of (request, rows of its work items)."""
+        batch, n = [], 0
+        rr = [r for r in self._active.values() if r.kind == 'rr' and r.state['icur'] < len(r.state['items'])]
+        while rr and n < self.step_items:
             nxt = []
+            share = max(1, (self.step_items - n) // len(rr))
             for r in rr:
-                q = r.state['items']
-                take = max(1, min(len(q), (self.step_items - len(batch)) // max(len(rr), 1)))
-                for _ in range(take):
-                    if not q or len(batch) >= self.step_items:
-                        break
-                    batch.append((r, q.popleft()))
-                if q:
+                items, c = r.state['items'], r.state['icur']
+                take = min(share, len(items) - c, self.step_items - n)
+                if take <= 0:
+                    break
+                batch.append((r, items[c:c + take]))
+                r.state['icur'] = c + take
+                n += take
+                if r.state['icur'] < len(items):
                     nxt.append(r)
             rr = nxt
         return batch
@@ -391,7 +408,7 @@ class RRServer:
                 for r in ts_work:
                     self._issued[r.rid] = r
                 for r in {id(r): r for r, _ in batch}.values():
-                    if not r.state['items']:
+                    if r.state['icur'] >= len(r.state['items']):
                         self._issued[r.rid] = r
             # completions, polled in issue order: stop at the few oldest still running
             pending = 0
@@ -471,11 +488,6 @@ class GpuExecutor:
         self.descs_h = self.descs_pin.numpy().view(self.desc_dtype)
         self.descs_d = torch.zeros(dsz, dtype=torch.uint8, device=self.device)
         self._dirty = set()
-        # item list: two pinned staging buffers used in turn; a buffer is
-        # rewritten once the copy that last read it has run
-        self.items_pin = [torch.zeros(self.MAX_ITEMS * 6 + 8, dtype=torch.int32, pin_memory=True) for _ in range(2)]
-        self.items_ev = [None, None]
-        self._istep = 0
         self.items_d = torch.zeros(self.MAX_ITEMS * 6 + 8, dtype=torch.int32, device=self.device)
         self.counter = torch.zeros(4, dtype=torch.int32, device=self.device)
         self.free_slots = list(range(self.MAX_REQ - 1, -1, -1))
@@ -631,21 +643,26 @@ class GpuExecutor:
                     isz = self.desc_dtype.itemsize
                     self.descs_d[lo * isz:hi * isz].copy_(self.descs_pin[lo * isz:hi * isz], non_blocking=True)
                     self._dirty.clear()
-                j = self._istep % 2
-                self._istep += 1
-                if self.items_ev[j] is not None:
-                    self.items_ev[j].synchronize()
-                pin = self.items_pin[j]
-                arr = pin.numpy()
-                n = len(batch)
-                arr[:n * 6] = np.array([(r.state['slot'], *w, 0) for r, w in batch], np.int32).reshape(-1)
-                arr[n * 6] = n
-                # items and their count in one copy; the count goes to its fixed slot
-                self.items_d[:n * 6].copy_(pin[:n * 6], non_blocking=True)
-                self.items_d[self.MAX_ITEMS * 6:self.MAX_ITEMS * 6 + 1].copy_(pin[n * 6:n * 6 + 1], non_blocking=True)
+                # the item list and its count go through the pinned ring (a
+                # region is reused only after its copy has run: no host wait)
+                n = sum(len(w) for _, w in batch)
+                nb = 4 * (n * 6 + 1)
+                lo = self.ring.alloc(nb)
+                buf = self.ring.np[lo:lo + nb].view(np.int32)
+                rows = buf[:n * 6].reshape(n, 6)
+                c = 0
+                for r, w in batch:
+                    rows[c:c + len(w), 0] = r.state['slot']
+                    rows[c:c + len(w), 1:5] = w
+                    c += len(w)
+                rows[:, 5] = 0
+                buf[n * 6] = n
+                src = self.ring.buf[lo:lo + nb].view(torch.int32)
+                self.items_d[:n * 6].copy_(src[:n * 6], non_blocking=True)
+                self.items_d[self.MAX_ITEMS * 6:self.MAX_ITEMS * 6 + 1].copy_(src[n * 6:n * 6 + 1], non_blocking=True)
                 cev = torch.cuda.Event()
                 cev.record(self.stream)
-                self.items_ev[j] = cev
+                self.ring.commit(lo, nb, cev)
                 self.graph.replay()
             ev = torch.cuda.Event()
             ev.record(self.stream)

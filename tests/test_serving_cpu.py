@@ -25,7 +25,7 @@ class FakeExecutor:
         self.log.append(('setup', req.rid))
 
     def step(self, batch, ts):
-        self.log.append(('step', [(r.rid, w) for r, w in batch], [r.rid for r in ts]))
+        self.log.append(('step', [(r.rid, tuple(w)) for r, ws in batch for w in ws], [r.rid for r in ts]))
 
     def start_copy(self, req):
         req.state['copy_at'] = len(self.log)
