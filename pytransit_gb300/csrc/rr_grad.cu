@@ -369,12 +369,26 @@ __global__ void __launch_bounds__(GRAD_THREADS) lnlike_kernel(GradArgs<R> A) {
   const int nsl = A.grad ? GS_C0 + A.npar : 1;
   for (int s = 0; s < nsl; ++s) {
     const int col = (s == GS_LNL) ? -1 : grad_col(s, A.nkc, A.nep, A.npar, pb, ep, s - GS_C0);
-    double v = (double)slot[s];
-    if (uni) {
+    if (!uni) {
+      if (slot[s] != R(0)) atomicAdd(&red[col + 1], (double)slot[s]);
+      continue;
+    }
+    if constexpr (sizeof(R) == 4) {
+      // FP32 (hi, lo) pairs summed with error-free two-sums: the warp sum is
+      // as accurate as an FP64 one without the FP64 pipe (1/64 rate)
+      float hi = slot[s], lo = 0.0f;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(FULL, hi, o), l2 = __shfl_down_sync(FULL, lo, o);
+        float sh, se;
+        two_sum(hi, h2, sh, se);
+        lo = lo + l2 + se;
+        hi = sh;
+      }
+      if (lane == 0 && (hi != 0.0f || lo != 0.0f)) atomicAdd(&red[col + 1], (double)hi + (double)lo);
+    } else {
+      double v = (double)slot[s];
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
       if (lane == 0 && v != 0.0) atomicAdd(&red[col + 1], v);
-    } else if (v != 0.0) {
-      atomicAdd(&red[col + 1], v);
     }
   }
   __syncthreads();
