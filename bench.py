@@ -447,7 +447,8 @@ def main():
     ap.add_argument("--npt", type=int, default=19700)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the precision and gradient workloads")
-    ap.add_argument("--workload", default="c1", choices=["c1", "serve"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "serve"],
+                    help="c1: the default line; c2 / c3: the precision / gradient workload alone; serve: Poisson stream")
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--nreq", type=int, default=300)
     ap.add_argument("--plain-sample", type=int, default=100000)
@@ -462,6 +463,14 @@ def main():
         return impl_reference(args, rank)
     if args.workload == "serve":
         return bench_serve(args) if rank == 0 else 0
+    if args.workload in ("c2", "c3"):
+        if rank == 0:
+            import torch
+            device = torch.device("cuda", 0)
+            torch.cuda.set_device(device)
+            fn = bench_c2 if args.workload == "c2" else bench_c3
+            print(json.dumps({"workload": args.workload, **fn(torch, device)}), flush=True)
+        return 0
 
     import torch
     import torch.distributed as dist
