@@ -310,6 +310,26 @@ def bench_c3(torch, device, steps=3):
             "timed": "lnlikelihood(grad=True) end to end (LD tables, prologue, fused lnL + adjoint), wall clock"}
 
 
+def bench_eclipse(torch, device, data, prm, steps=3):
+    """The secondary-eclipse model (FP64) on the default workload's data and
+    population (8192 pv x 19,700 times): model points/s."""
+    from pytransit_gb300 import EclipseModel
+    m = EclipseModel(device=device)
+    m.set_data(data["time"], lcids=data["lcids"], pbids=data["pbids"])
+    args = (prm["k"][:, 0], prm["t0"], prm["p"], prm["a"], prm["i"], prm["e"], prm["w"])
+    m.evaluate(*args, copy=False)
+    torch.cuda.synchronize(device)
+    t = time.perf_counter()
+    for _ in range(steps):
+        out = m.evaluate(*args, copy=False)
+    torch.cuda.synchronize(device)
+    dt = (time.perf_counter() - t) / steps
+    k2 = torch.as_tensor(np.pi * prm["k"][:, :1] ** 2).to(device)
+    return {"workload": "EclipseModel.evaluate(copy=False), 8192 pv x 19700 times, FP64, parameters uploaded each "
+                        "call", "points_per_s": out.numel() / dt, "ms": dt * 1e3,
+            "in_eclipse_fraction": float((out < k2 - 1e-12).double().mean().item())}
+
+
 def c4_requests(nreq, seed=4):
     """The serving mix: npv log-uniform [1, 4096], npt log-uniform [500, 1e5],
     nsamples in {1, 5, 10}, LD in {quadratic, power-2, nonlinear}, 20 %
@@ -658,6 +678,7 @@ def main():
     if rank == 0 and not args.no_extra:
         line["c2_precision"] = bench_c2(torch, device)
         line["c3_gradient"] = bench_c3(torch, device)
+        line["eclipse"] = bench_eclipse(torch, device, data, prm)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_baseline(data, prm)
     if rank == 0:

@@ -243,6 +243,30 @@ int rr_ma_quad_flux_f64(const double *times, int npt, const double *k, int nkc, 
                         const int32_t *epids, const int32_t *nsamples, const double *exptimes, const double *ldc,
                         const void *workspace, double *flux, int ldflux, void *stream);
 
+/* ---- secondary eclipse ----------------------------------------------------- */
+
+/* Workspace of rr_eclipse_f64 / rr_es_f64 (one record per parameter vector). */
+size_t rr_eclipse_workspace_bytes(int npv);
+/* eclipse_model (pytransit/models/roadrunner/model_eclipse.py:12-81), FP64: the
+ * visible area of the planet disk, flux[npv, ldflux] = pi k^2 outside the
+ * eclipse and the mean over the exposure samples of pi k^2 - A(1, k, z)
+ * inside it; k[npv], t0[npv, ldt0] per epoch (epids[nlc]), rstar[npv] in
+ * solar radii for the light travel time.  The orbit is expanded about
+ * mid-eclipse (the mean-anomaly offset of orbits_py.eclipse_phase) and the
+ * eclipse shifted by the light travel time across the orbit; invalid
+ * parameter vectors give NaN rows. */
+int rr_eclipse_f64(const double *times, int npt, const double *k, const double *t0, int ldt0, const double *p,
+                   const double *a, const double *inc, const double *e, const double *w, const double *rstar,
+                   int npv, int nlc, const int32_t *lcids, const int32_t *epids, const int32_t *nsamples,
+                   const double *exptimes, void *workspace, size_t workspace_bytes, double *flux, int ldflux,
+                   void *stream);
+/* esmodel (model_ecspec.py:13-63), FP64: flux[npv, npb, ldflux] for the flux
+ * ratios fratio[npv, npb], one zero epoch t0[npv], nsamples0 / exptime0. */
+int rr_es_f64(const double *times, int npt, const double *k, const double *t0, const double *p, const double *a,
+              const double *inc, const double *e, const double *w, const double *rstar, const double *fratio,
+              int npv, int npb, int nsamples0, double exptime0, void *workspace, size_t workspace_bytes,
+              double *flux, int ldflux, void *stream);
+
 /* ---- sampler parameter mapping -------------------------------------------- */
 
 /* BaseLPF.transit_model's parameter mapping (pytransit/lpf/lpf.py:435-443) on

@@ -85,6 +85,14 @@ def lib():
         L.rro_ma_quad_z.argtypes = [C.c_double] * 4
         L.rro_ma_quad_z.restype = C.c_double
         L.rro_ma_quad_z_v.argtypes = [_d, C.c_int, C.c_double, C.c_double, C.c_double, _d]
+        L.rro_eclipse_time_offset.argtypes = [C.c_double] * 4
+        L.rro_eclipse_time_offset.restype = C.c_double
+        L.rro_eclipse_ltt.argtypes = [C.c_double] * 6
+        L.rro_eclipse_ltt.restype = C.c_double
+        L.rro_eclipse_full.argtypes = [_d, C.c_int, _d, _d, C.c_int, _d, _d, _d, _d, _d, C.c_int, C.c_double,
+                                       C.c_int, _i, _i, _i, _d, _d]
+        L.rro_es_full.argtypes = [_d, C.c_int, _d, _d, _d, _d, _d, _d, _d, _d, _d, C.c_int, C.c_int, C.c_int,
+                                  C.c_double, _d]
         _LIB = L
     return _LIB
 
@@ -252,6 +260,31 @@ def ma_quad_z(z, k, u1, u2):
     z = _f64(np.atleast_1d(z))
     out = np.empty_like(z)
     lib().rro_ma_quad_z_v(_dp(z), z.size, float(k), float(u1), float(u2), _dp(out))
+    return out
+
+
+def eclipse_full(times, k, t0, p, a, i, e, w, rstar, lcids, epids, nsamples, exptimes):
+    """eclipse_model (pytransit/models/roadrunner/model_eclipse.py:12-81): the
+    visible planet area [npv, npt]; k[npv], t0[npv, nep]."""
+    times, k, t0 = _f64(times), _f64(np.atleast_1d(k)), _f64(np.atleast_2d(t0))
+    p, a, i, e, w = (_f64(np.broadcast_to(np.atleast_1d(x), k.shape)) for x in (p, a, i, e, w))
+    lcids, epids, nsamples = _i32(lcids), _i32(epids), _i32(nsamples)
+    exptimes = _f64(exptimes)
+    out = np.empty((k.size, times.size))
+    lib().rro_eclipse_full(_dp(times), times.size, _dp(k), _dp(t0), t0.shape[1], _dp(p), _dp(a), _dp(i), _dp(e),
+                           _dp(w), k.size, float(rstar), int(epids.size), _ip(lcids), _ip(epids), _ip(nsamples),
+                           _dp(exptimes), _dp(out))
+    return out
+
+
+def es_full(times, k, t0, p, a, i, e, w, rstar, fratio, nsamples, exptime):
+    """esmodel (pytransit/models/roadrunner/model_ecspec.py:13-63): flux[npv, npb, npt]."""
+    times, k = _f64(times), _f64(np.atleast_1d(k))
+    t0, p, a, i, e, w, rstar = (_f64(np.broadcast_to(np.atleast_1d(x), k.shape)) for x in (t0, p, a, i, e, w, rstar))
+    fratio = _f64(np.atleast_2d(fratio))
+    out = np.empty((k.size, fratio.shape[1], times.size))
+    lib().rro_es_full(_dp(times), times.size, _dp(k), _dp(t0), _dp(p), _dp(a), _dp(i), _dp(e), _dp(w), _dp(rstar),
+                      _dp(fratio), k.size, fratio.shape[1], int(nsamples), float(exptime), _dp(out))
     return out
 
 

@@ -351,14 +351,14 @@ double rro_sep_c(double t, const double *c)
 }
 
 /* Contact-point bisection as pytransit/orbits/taylor_z.py:299-328
- * (initial bracket [0, s*2/vx], tolerance 1e-6 d, at most 100 steps), with z
+ * (initial bracket [0, s*2/|vx|], tolerance 1e-6 d, at most 100 steps), with z
  * from sep_c (time measured from conjunction, no period fold). */
 static double rro_contact(double k, int point, const double *c)
 {
     double s = (point == 1 || point == 2) ? -1.0 : 1.0;
     double zt = (point == 1 || point == 4) ? 1.0 + k : 1.0 - k;
     double t0 = 0.0;
-    double t2 = s * 2.0 / c[1];
+    double t2 = s * 2.0 / fabs(c[1]);   /* sky speed: dx/dt < 0 about an eclipse */
     double t1 = 0.5 * t2;
     double z0 = rro_sep_c(t0, c) - zt;
     double z1 = rro_sep_c(t1, c) - zt;
@@ -770,4 +770,128 @@ double rro_ma_quad_z(double z, double k, double u1, double u2)
 void rro_ma_quad_z_v(const double *z, int n, double k, double u1, double u2, double *flux)
 {
     for (int i = 0; i < n; ++i) flux[i] = rro_ma_quad_z(z[i], k, u1, u2);
+}
+
+/* ------------------------------------------------------------------ */
+/* RoadRunner secondary eclipse: eclipse_model (model_eclipse.py:12-81) */
+/* and the spectroscopic esmodel (model_ecspec.py:13-63)               */
+/* ------------------------------------------------------------------ */
+
+/* Time from mid-transit to mid-eclipse (meepmeep's eclipse_time_offset, not
+ * in the reference; restated as the reference's own eclipse_phase,
+ * pytransit/orbits/orbits_py.py:544-555): from the mean anomalies at the two
+ * conjunctions, wrapped to (0, p]. */
+double rro_eclipse_time_offset(double p, double inc, double e, double w)
+{
+    (void)inc;
+    double se = sqrt(1.0 - e * e);
+    double etr = atan2(se * sin(0.5 * RRO_PI - w), e + cos(0.5 * RRO_PI - w));
+    double eec = atan2(se * sin(0.5 * RRO_PI + RRO_PI - w), e + cos(0.5 * RRO_PI + RRO_PI - w));
+    double mtr = etr - e * sin(etr), mec = eec - e * sin(eec);
+    double ph = (mec - mtr) * p / (2.0 * RRO_PI);
+    return ph > 0.0 ? ph : p + ph;
+}
+
+/* Light travel time of the eclipse relative to the transit in days (meepmeep's
+ * eclipse_light_travel_time, not in the reference; restated from the
+ * geometry): (r_transit + r_eclipse) sin i stellar radii of rstar solar radii
+ * (IAU nominal 6.957e8 m) over c. */
+double rro_eclipse_ltt(double p, double a, double inc, double e, double w, double rstar)
+{
+    (void)p;
+    double r_tr = a * (1.0 - e * e) / (1.0 + e * cos(0.5 * RRO_PI - w));
+    double r_ec = a * (1.0 - e * e) / (1.0 + e * cos(1.5 * RRO_PI - w));
+    return (r_tr + r_ec) * sin(inc) * rstar * 6.957e8 / 299792458.0 / 86400.0;
+}
+
+/* eclipse_model: the visible area of the planet disk, pi k^2 outside the
+ * eclipse bounding box (padded by 0.003 d + exptime), else the mean over the
+ * exposure samples of pi k^2 - A(1, k, z), z from the Taylor series about
+ * mid-eclipse; t0[npv, nep] per epoch; NaN rows for a NaN or <= 1, e < 0. */
+void rro_eclipse_full(const double *times, int npt, const double *k, const double *t0, int nep, const double *p,
+                      const double *a, const double *inc, const double *e, const double *w, int npv, double rstar,
+                      int nlc, const int32_t *lcids, const int32_t *epids, const int32_t *nsamples,
+                      const double *exptimes, double *flux)
+{
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int ipv = 0; ipv < npv; ++ipv) {
+        double *fl = flux + (size_t)ipv * npt;
+        if (isnan(a[ipv]) || a[ipv] <= 1.0 || e[ipv] < 0.0) {
+            for (int j = 0; j < npt; ++j) fl[j] = NAN;
+            continue;
+        }
+        double shift = rro_eclipse_time_offset(p[ipv], inc[ipv], e[ipv], w[ipv]);
+        double c[10];
+        rro_solve2d(shift, p[ipv], a[ipv], inc[ipv], e[ipv], w[ipv], c);
+        double ltt = rro_eclipse_ltt(p[ipv], a[ipv], inc[ipv], e[ipv], w[ipv], rstar);
+        double bt1, bt4;
+        rro_bounding_box(k[ipv], c, &bt1, &bt4);
+        double pik2 = RRO_PI * (k[ipv] * k[ipv]);
+        for (int j = 0; j < npt; ++j) {
+            int ilc = lcids[j];
+            double te = t0[(size_t)ipv * nep + epids[ilc]] + shift + ltt;
+            double epoch = floor((times[j] - te + 0.5 * p[ipv]) / p[ipv]);
+            double tc = times[j] - (te + epoch * p[ipv]);
+            double lo = bt1 - (0.003 + exptimes[ilc]), hi = bt4 + (0.003 + exptimes[ilc]);
+            (void)nlc;
+            if (!(lo <= tc && tc <= hi)) {
+                fl[j] = pik2;
+            } else {
+                double f = 0.0;
+                int ns = nsamples[ilc];
+                for (int is = 1; is < ns + 1; ++is) {
+                    double toff = exptimes[ilc] * ((is - 0.5) / ns - 0.5);
+                    double z = rro_sep_c(tc + toff, c), kap;
+                    f += pik2 - rro_ccia(1.0, k[ipv], z, &kap);
+                }
+                fl[j] = f / ns;
+            }
+        }
+    }
+}
+
+/* esmodel: flux[npv, npb, npt] = 1 outside the box (padded by 0.0015 d +
+ * exptime), else the mean over the samples of
+ * 1 - (f_b A(1, k, z) / pi) / (1 + f_b k^2); one zero epoch t0[npv], the
+ * first light curve's nsamples and exptime, rstar[npv]. */
+void rro_es_full(const double *times, int npt, const double *k, const double *t0, const double *p, const double *a,
+                 const double *inc, const double *e, const double *w, const double *rstar, const double *fratio,
+                 int npv, int npb, int nsamples, double exptime, double *flux)
+{
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int ipv = 0; ipv < npv; ++ipv) {
+        double *fl = flux + (size_t)ipv * npb * npt;
+        if (isnan(a[ipv]) || a[ipv] <= 1.0 || e[ipv] < 0.0) {
+            for (size_t j = 0; j < (size_t)npb * npt; ++j) fl[j] = NAN;
+            continue;
+        }
+        double shift = rro_eclipse_time_offset(p[ipv], inc[ipv], e[ipv], w[ipv]);
+        double c[10];
+        rro_solve2d(shift, p[ipv], a[ipv], inc[ipv], e[ipv], w[ipv], c);
+        double ltt = rro_eclipse_ltt(p[ipv], a[ipv], inc[ipv], e[ipv], w[ipv], rstar[ipv]);
+        double te = t0[ipv] + shift + ltt;
+        double bt1, bt4;
+        rro_bounding_box(k[ipv], c, &bt1, &bt4);
+        bt1 -= 0.0015 + exptime;
+        bt4 += 0.0015 + exptime;
+        for (int j = 0; j < npt; ++j) {
+            double epoch = floor((times[j] - te + 0.5 * p[ipv]) / p[ipv]);
+            double tc = times[j] - (te + epoch * p[ipv]);
+            if (!(bt1 <= tc && tc <= bt4)) {
+                for (int b = 0; b < npb; ++b) fl[(size_t)b * npt + j] = 1.0;
+                continue;
+            }
+            for (int b = 0; b < npb; ++b) fl[(size_t)b * npt + j] = 0.0;
+            for (int is = 1; is < nsamples + 1; ++is) {
+                double toff = exptime * ((is - 0.5) / nsamples - 0.5);
+                double z = rro_sep_c(tc + toff, c), kap;
+                double ar = rro_ccia(1.0, k[ipv], z, &kap);
+                for (int b = 0; b < npb; ++b) {
+                    double f = fratio[(size_t)ipv * npb + b];
+                    fl[(size_t)b * npt + j] += 1.0 - (f * ar / RRO_PI) / (1.0 + f * (k[ipv] * k[ipv]));
+                }
+            }
+            for (int b = 0; b < npb; ++b) fl[(size_t)b * npt + j] /= nsamples;
+        }
+    }
 }

@@ -311,6 +311,54 @@ __device__ inline void basis_coefs(int law, const double* pv, int npar, double* 
 // r'' = -mu r/|r|^3.  c[0..4] are the x coefficients, c[5..9] the y ones
 // (x(t) = sum c[j] t^j, layout of gdmodel.py:441-442); sky axes as
 // taylor_z.py:62-76.
+// Eccentric anomaly from the mean anomaly by Newton's method, |err| <= 1e-8
+// (ea_newton_s, pytransit/orbits/orbits_py.py:145-154).
+__device__ inline double ea_newton(double M, double e) {
+  double E = M, err = 0.05;
+  for (int k = 0; fabs(err) > 1e-8 && k < 1000; ++k) {
+    err = E - e * sin(E) - M;
+    E = E - err / (1.0 - e * cos(E));
+  }
+  return E;
+}
+
+// solve2d about t = phase (days from mid-transit; the mid-eclipse for the
+// eclipse models): the Keplerian state at that time (mean anomaly from the
+// one at conjunction, f = pi/2 - w, plus n phase), then the Taylor jet of
+// solve2d_conj below.
+__device__ inline void solve2d_phase(double phase, double p, double a, double inc, double e, double w, double* c) {
+  const double n = 2.0 * PI / p;
+  const double se = sqrt(1.0 - e * e);
+  const double f0 = 0.5 * PI - w;
+  const double E0 = atan2(se * sin(f0), e + cos(f0));
+  const double M = E0 - e * sin(E0) + n * phase;
+  const double E = ea_newton(M, e);
+  const double f = atan2(se * sin(E) / (1.0 - e * cos(E)), (cos(E) - e) / (1.0 - e * cos(E)));
+  const double sf = sin(f), cf = cos(f);
+  const double cth = cos(w + f), sth = sin(w + f);
+  const double r = a * (1.0 - e * e) / (1.0 + e * cf);
+  const double vr = n * a * e * sf / se;
+  const double vt = n * a * (1.0 + e * cf) / se;
+  double P0x = r * cth, P0y = r * sth;
+  double P1x = vr * cth - vt * sth, P1y = vr * sth + vt * cth;
+  const double mu = n * n * a * a * a;
+  const double alpha = -1.5;
+  const double q0 = P0x * P0x + P0y * P0y;
+  const double q1 = 2.0 * (P0x * P1x + P0y * P1y);
+  const double s0 = 1.0 / (q0 * sqrt(q0));
+  const double P2x = -mu * s0 * P0x / 2.0, P2y = -mu * s0 * P0y / 2.0;
+  const double s1 = alpha * q1 * s0 / q0;
+  const double P3x = -mu * (s0 * P1x + s1 * P0x) / 6.0;
+  const double P3y = -mu * (s0 * P1y + s1 * P0y) / 6.0;
+  const double q2 = 2.0 * (P0x * P2x + P0y * P2y) + (P1x * P1x + P1y * P1y);
+  const double s2 = ((alpha - 1.0) * q1 * s1 + 2.0 * alpha * q2 * s0) / (2.0 * q0);
+  const double P4x = -mu * (s0 * P2x + s1 * P1x + s2 * P0x) / 12.0;
+  const double P4y = -mu * (s0 * P2y + s1 * P1y + s2 * P0y) / 12.0;
+  const double ci = cos(inc);
+  c[0] = -P0x; c[1] = -P1x; c[2] = -P2x; c[3] = -P3x; c[4] = -P4x;
+  c[5] = -ci * P0y; c[6] = -ci * P1y; c[7] = -ci * P2y; c[8] = -ci * P3y; c[9] = -ci * P4y;
+}
+
 __device__ inline void solve2d_conj(double p, double a, double inc, double e, double w, double* c) {
   double n = 2.0 * PI / p;
   double se = sqrt(1.0 - e * e);
@@ -351,7 +399,7 @@ __device__ inline double contact_point(double k, int point, const double* c) {
   double s = (point == 1 || point == 2) ? -1.0 : 1.0;
   double zt = (point == 1 || point == 4) ? 1.0 + k : 1.0 - k;
   double t0 = 0.0;
-  double t2 = s * 2.0 / c[1];
+  double t2 = s * 2.0 / fabs(c[1]);   // the sky speed (dx/dt < 0 about an eclipse)
   double t1 = 0.5 * t2;
   double z0 = sep_c_f64(t0, c) - zt;
   double z1 = sep_c_f64(t1, c) - zt;
@@ -401,7 +449,7 @@ __device__ inline float contact_point_f32(float k, int point, const float* c) {
   const float s = (point == 1 || point == 2) ? -1.0f : 1.0f;
   const float zt = (point == 1 || point == 4) ? 1.0f + k : 1.0f - k;
   float t0 = 0.0f;
-  float t2 = s * 2.0f / c[1];
+  float t2 = s * 2.0f / fabsf(c[1]);
   float t1 = 0.5f * t2;
   float z0 = sep_c_f32(t0, c) - zt;
   float z1 = sep_c_f32(t1, c) - zt;

@@ -19,7 +19,8 @@ RoadRunnerModel.__init__/set_data/evaluate (rrmodel.py), rr_full and rr_simple
 (common.py), the LD laws (numba/ldmodels.py), LDModel (ldmodel.py),
 TransitModel.set_data (transitmodel.py), TransmissionSpectroscopyModel /
 tsmodel_serial (tsmodel.py, model_trspec.py) and the Mandel & Agol quadratic
-model used as the independent cross-check (numba/ma_quadratic_nb.py).
+model used as the independent cross-check (numba/ma_quadratic_nb.py) and the
+secondary-eclipse kernels (model_eclipse.py, model_ecspec.py).
 """
 import os
 import sys
@@ -339,8 +340,58 @@ def case_lpf_map():
          inc=i_from_ba(pv[:, 3], a), ldc=map_ldc(pv[:, 5:]).reshape(npv, npb, 2))
 
 
+def case_eclipse():
+    """The reference's RoadRunner secondary-eclipse kernels, eclipse_model
+    (model_eclipse.py) and esmodel (model_ecspec.py), on the restated orbit
+    layer (shim: solve2d about mid-eclipse, eclipse_time_offset,
+    eclipse_light_travel_time): the reference test's canonical case, a
+    multi-light-curve BJD-scale set with supersampling, epochs, eccentric
+    orbits and invalid rows, and the spectroscopic variant."""
+    from pytransit.models.roadrunner.model_eclipse import eclipse_model
+    from pytransit.models.roadrunner.model_ecspec import esmodel
+    out = {}
+    times = np.linspace(-0.5, 3.5, 5000)
+    out["canon_time"] = times
+    out["canon_flux"] = eclipse_model(times, np.array([0.1]), np.full((1, 1), 0.0), np.array([2.0]), np.array([8.0]),
+                                      np.array([np.pi / 2]), np.array([0.0]), np.array([0.0]), 1.0, 1,
+                                      np.zeros(times.size, np.int64), np.zeros(1, np.int64), np.ones(1, np.int64),
+                                      np.zeros(1))
+    rng = np.random.default_rng(53)
+    T = 2459000.0
+    t_a = T + np.arange(0, 6.0, 2 / 1440)
+    t_b = T + 7.0 + np.arange(0, 5.0, 10 / 1440)
+    time = np.concatenate([t_a, t_b])
+    lcids = np.concatenate([np.zeros(t_a.size, np.int64), np.ones(t_b.size, np.int64)])
+    epids = np.array([0, 1])
+    nsamples = np.array([1, 5])
+    exptimes = np.array([0.0, 10 / 1440])
+    npv = 12
+    k = rng.uniform(0.05, 0.15, npv)
+    t0 = T + 0.2 + rng.normal(0, 1e-3, npv)
+    t0 = np.stack([t0, t0 + rng.normal(0, 0.005, npv)], -1)
+    p = rng.uniform(1.0, 4.0, npv)
+    a = rng.uniform(4.0, 12.0, npv)
+    inc = np.arccos(rng.uniform(0, 0.7, npv) / a)
+    e = np.concatenate([np.zeros(4), rng.uniform(0, 0.3, npv - 4)])
+    w = rng.uniform(0, 2 * np.pi, npv)
+    a[5] = 0.8          # a <= 1: NaN row
+    out.update(dict(time=time, lcids=lcids, epids=epids, nsamples=nsamples, exptimes=exptimes, k=k, t0=t0, p=p, a=a,
+                    inc=inc, e=e, w=w, rstar=1.3))
+    out["flux"] = eclipse_model(time, k, t0, p, a, inc, e, w, 1.3, 2, lcids, epids, nsamples, exptimes)
+    # spectroscopic variant: per-pv rstar, npb flux ratios, the first light curve's sampling
+    npv_s, npb = 6, 7
+    ts = T + np.arange(-1.0, 4.0, 5 / 1440)
+    fr = rng.uniform(1e-4, 5e-3, (npv_s, npb))
+    rs = rng.uniform(0.5, 2.0, npv_s)
+    es = dict(k=k[:npv_s], t0=t0[:npv_s, 0], p=p[:npv_s], a=a[:npv_s], inc=inc[:npv_s], e=e[:npv_s], w=w[:npv_s])
+    out.update({f"es_{n}": v for n, v in es.items()})
+    out.update(dict(es_time=ts, es_rstar=rs, es_fratio=fr))
+    out["es_flux"] = esmodel(ts, es["k"], es["t0"], es["p"], es["a"], es["inc"], es["e"], es["w"], rs, fr, 3, 0.01)
+    save("eclipse", **out)
+
+
 if __name__ == "__main__":
     for f in (case_tables, case_c0, case_multi, case_power2, case_laws, case_user_ld, case_klims,
-              case_simple, case_ts, case_ma_quadratic, case_lpf_map):
+              case_simple, case_ts, case_ma_quadratic, case_lpf_map, case_eclipse):
         print(f.__name__)
         f()

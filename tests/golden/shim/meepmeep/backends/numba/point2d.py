@@ -11,7 +11,9 @@ days from conjunction; ``sep_c(t, c)`` the sky separation; and
 
 The Taylor coefficients are the exact time derivatives of the Keplerian sky
 position (a Taylor jet of r'' = -mu r / |r|^3), the contact times follow the
-bisection of pytransit/orbits/taylor_z.py:299-328 on the Taylor polynomial.
+bisection of pytransit/orbits/taylor_z.py:299-328 on the Taylor polynomial
+(bracketed with the sky speed |dx/dt|, so it also serves an expansion about
+mid-eclipse, where dx/dt < 0).
 The oracle (oracle/rr_oracle.c) and the CUDA orbit kernel implement the same
 statement; agreement with meepmeep's own numbers is not pinned.
 """
@@ -82,7 +84,7 @@ def find_contact_point(k, point, c):
     s = -1.0 if point in (1, 2) else 1.0
     zt = 1.0 + k if point in (1, 4) else 1.0 - k
     t0 = 0.0
-    t2 = s * 2.0 / c[0, 1]
+    t2 = s * 2.0 / abs(c[0, 1])     # the sky speed: x velocity is negative about an eclipse
     t1 = 0.5 * t2
     z0 = sep_c(t0, c) - zt
     z1 = sep_c(t1, c) - zt

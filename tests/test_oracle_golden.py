@@ -214,3 +214,34 @@ def test_ma_quadratic_matches_reference(golden):
             assert np.array_equal(np.isnan(got), np.isnan(want)), (k, u)
             m = ~np.isnan(want)
             assert np.abs(got[m] - want[m]).max() <= 1e-12, (k, u)
+
+
+# --- secondary eclipse (model_eclipse.py, model_ecspec.py) -----------------
+
+def test_eclipse_oracle_matches_reference(golden):
+    g = golden("eclipse")
+    f = oracle.eclipse_full(g["canon_time"], [0.1], [[0.0]], 2.0, 8.0, np.pi / 2, 0.0, 0.0, 1.0,
+                            np.zeros(g["canon_time"].size, int), [0], [1], [0.0])
+    assert np.abs(f - g["canon_flux"]).max() <= 1e-12
+    f = oracle.eclipse_full(g["time"], g["k"], g["t0"], g["p"], g["a"], g["inc"], g["e"], g["w"], float(g["rstar"]),
+                            g["lcids"], g["epids"], g["nsamples"], g["exptimes"])
+    assert np.array_equal(np.isnan(f), np.isnan(g["flux"]))
+    m = ~np.isnan(g["flux"])
+    assert np.abs(f[m] - g["flux"][m]).max() <= 1e-12
+    f = oracle.es_full(g["es_time"], g["es_k"], g["es_t0"], g["es_p"], g["es_a"], g["es_inc"], g["es_e"], g["es_w"],
+                       g["es_rstar"], g["es_fratio"], 3, 0.01)
+    assert np.array_equal(np.isnan(f), np.isnan(g["es_flux"]))
+    m = ~np.isnan(g["es_flux"])
+    assert np.abs(f[m] - g["es_flux"][m]).max() <= 1e-12
+
+
+def test_eclipse_reference_test_properties():
+    """The reference's own checks (tests/test_roadrunner_eclipse.py): out of
+    eclipse the full planet area pi k^2, the eclipse near t = p/2 = 1 d, total
+    (area ~0) for a non-grazing orbit."""
+    times = np.linspace(-0.5, 3.5, 5000)
+    f = oracle.eclipse_full(times, [0.1], [[0.0]], 2.0, 8.0, np.pi / 2, 0.0, 0.0, 1.0, np.zeros(5000, int), [0], [1],
+                            [0.0])[0]
+    assert abs(f.max() - np.pi * 0.01) < 1e-6
+    assert f[np.argmin(np.abs(times - 1.0))] < np.pi * 0.01 - 1e-4
+    assert f.min() < 1e-3
