@@ -501,16 +501,7 @@ def main():
     if world > 1:
         dist.init_process_group("nccl", device_id=device)
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    from pytransit_gb300.sharding import barrier, max_over_ranks
 
     # Each rank evaluates its own population (weak scaling, no collective on the data path).
     data, prm = workload(args.npv, args.npt, seed=1234 + rank)
