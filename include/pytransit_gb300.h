@@ -158,6 +158,22 @@ int rr_prepare_split(double t_ref, double t_absmax, const double *k, int nkc, co
                      const float *basis, int nb);
 int rr_flux_split(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb, int ng,
                   double dg, const void *workspace, float *flux, int ldflux, void *stream);
+/* rr_ld_tables_f32 followed by rr_prepare_split, as one launch for the
+ * affine laws with an analytic disk integral (uniform, linear, quadratic,
+ * quadratic-tri) given their basis tables: ldp[npv, npb, nz] and
+ * istar[npv, npb] are written as rr_ld_tables_f32 writes them, and the
+ * workspace is filled as rr_prepare_split fills it (the LD profile of
+ * rrmodel.py:212-227 and the prologue of model_full.py:39-71).  For other
+ * laws, no basis, or npb * (npar + 1) > 128, the two stages run one after
+ * the other with the same arguments. */
+int rr_prepare_split_ld(double t_ref, double t_absmax, const double *k, int nkc, const double *t0, int ldt0,
+                        int nep, const double *p, const double *a, const double *inc, const double *e,
+                        const double *w, int npv, int nlc, int npb, const int32_t *pbids,
+                        const int32_t *epids, const int32_t *nsamples, const double *exptimes, int law,
+                        const double *ldc, int npar, const double *mu, int nz, const float *basis, int nb,
+                        const float *weights, int nk, int ng, double dk, double kmin, double kmax,
+                        const double *z_edges, float *ldp, float *istar, void *workspace,
+                        size_t workspace_bytes, void *stream);
 /* rr_flux_split for the parameter vectors [pv0, pv1) of a workspace prepared
  * for npv: flux[pv1 - pv0, ldflux] holds those rows.  Lets a caller compute
  * the flux in pv chunks and move each chunk to the host while the next one

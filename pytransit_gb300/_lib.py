@@ -52,6 +52,9 @@ def _sig(L):
     L.rr_prepare_split.argtypes = ([_d, _d, _vp, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp,
                                     _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _vp, _vp, _sz, _vp,
                                     _i, _vp, _i, _vp, _i])
+    L.rr_prepare_split_ld.argtypes = ([_d, _d, _vp, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp,
+                                       _vp, _vp, _vp, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i, _i, _d, _d, _d,
+                                       _vp, _vp, _vp, _vp, _sz, _vp])
     L.rr_flux_split.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _vp, _i, _vp]
     L.rr_flux_split_range.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
     L.rr_ts_workspace_bytes.argtypes = [_i, _i, _i, _i]

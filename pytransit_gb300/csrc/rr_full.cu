@@ -178,6 +178,34 @@ __global__ void basis_tables_kernel(int law, int nb, const double* __restrict__ 
 // and applied to ldp, as the generic kernel does.
 constexpr int MAX_BASIS = 16;
 
+// Row g of the LD means of one pv for every passband from the 2D weight table
+// built at k in FP64 (calculate_weights_2d, common.py:153-185): the k-outside-
+// the-tables case of the affine-law kernels.  ldp_pv = the pv's [npb][nz]
+// profiles, out = its [npb][ng] means.
+template <typename R>
+__device__ inline void ldm_direct_g(double k, int g, int ng, int nz, const double* __restrict__ ze,
+                                    const R* ldp_pv, int npb, R* out) {
+  const double gstep = (1.0 - 1e-7) / (double)(ng - 1);
+  double gg = (double)g * gstep;
+  if (g == ng - 1) gg = 1.0 - 1e-7;
+  const double bb = gg * (1.0 + k);
+  double w[64];
+  double a0 = cci_acos(ze[0], k, bb), s = a0;
+  w[0] = a0;
+  for (int z = 1; z < nz; ++z) {
+    const double a1 = cci_acos(ze[z], k, bb);
+    w[z] = a1 - a0;
+    a0 = a1;
+    s += w[z];
+  }
+  for (int pb = 0; pb < npb; ++pb) {
+    const R* l = ldp_pv + (size_t)pb * nz;
+    double acc = 0.0;
+    for (int z = 0; z < nz; ++z) acc += (w[z] / s) * (double)l[z];
+    out[(size_t)pb * ng + g] = (R)acc;
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(128)
 ldm_basis_kernel(int law, const double* __restrict__ ldc, int npar, int npb, const double* __restrict__ kw,
@@ -224,27 +252,8 @@ ldm_basis_kernel(int law, const double* __restrict__ ldc, int npar, int npb, con
     }
   } else {
     const double k = kw[(size_t)pv * kw_stride];
-    const double gstep = (1.0 - 1e-7) / (double)(ng - 1);
-    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-      double gg = (double)g * gstep;
-      if (g == ng - 1) gg = 1.0 - 1e-7;
-      const double bb = gg * (1.0 + k);
-      double w[64];
-      double a0 = cci_acos(ze[0], k, bb), s = a0;
-      w[0] = a0;
-      for (int z = 1; z < nz; ++z) {
-        const double a1 = cci_acos(ze[z], k, bb);
-        w[z] = a1 - a0;
-        a0 = a1;
-        s += w[z];
-      }
-      for (int pb = 0; pb < npb; ++pb) {
-        const R* l = ldp + ((size_t)pv * npb + pb) * nz;
-        double acc = 0.0;
-        for (int z = 0; z < nz; ++z) acc += (w[z] / s) * (double)l[z];
-        out[(size_t)pb * ng + g] = (R)acc;
-      }
-    }
+    for (int g = threadIdx.x; g < ng; g += blockDim.x)
+      ldm_direct_g(k, g, ng, nz, ze, ldp + (size_t)pv * npb * nz, npb, out);
   }
 }
 
@@ -264,15 +273,34 @@ struct OrbitArgs {
   float *orb32, *lc32;
   const float* istar32;
   double t_ref, t_absmax;
+  // split path with the LD profile evaluated here rather than read from
+  // ldp / istar32 (the fused prologue): the law's coefficients ldc[npv, npb,
+  // npar] and the mu grid, taken as FP32 as ld_tables_kernel<float> takes them
+  int ld_direct, law, npar;
+  const double *ldc, *mu;
 };
 
+constexpr int ORB_MAX_LDPAR = 4;   // coefficients per passband of the fused prologue's laws
+
+// FP32 coefficients of (pv, pb), as ld_tables_kernel<float> converts them.
+__device__ inline void ld_coefs_f32(const OrbitArgs& A, int pv, int pb, float* c) {
+  const double* src = A.ldc + ((size_t)pv * A.npb + pb) * A.npar;
+#pragma unroll
+  for (int i = 0; i < ORB_MAX_LDPAR; ++i) c[i] = i < A.npar ? (float)src[i] : 0.0f;
+}
+
 template <bool SPLIT>
-__global__ void orbit_kernel(OrbitArgs A) {
-  int pv = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pv >= A.npv) return;
+__device__ __forceinline__ void orbit_pv(const OrbitArgs& A, int pv) {
   double a = A.a[pv], e = A.e[pv], p = A.p[pv];
-  bool ldbad = A.ldp_is_f32 ? isnan(((const float*)A.ldp)[(size_t)pv * A.npb * A.nz])
-                            : isnan(((const double*)A.ldp)[(size_t)pv * A.npb * A.nz]);
+  bool ldbad;
+  if (SPLIT && A.ld_direct) {
+    float c[ORB_MAX_LDPAR];
+    ld_coefs_f32(A, pv, 0, c);
+    ldbad = isnan(ld_value<float>(A.law, (float)A.mu[0], c, A.npar));
+  } else {
+    ldbad = A.ldp_is_f32 ? isnan(((const float*)A.ldp)[(size_t)pv * A.npb * A.nz])
+                         : isnan(((const double*)A.ldp)[(size_t)pv * A.npb * A.nz]);
+  }
   bool valid = !(isnan(a) || a <= 1.0 || e < 0.0 || ldbad);
   double c[10];
   float cf[10];
@@ -323,7 +351,14 @@ __global__ void orbit_kernel(OrbitArgs A) {
     const float d0h = __double2float_rn(d0);
     const double kk = A.k[(size_t)pv * A.nkc + (A.nkc == A.npb ? pb : 0)];
     // a non-finite disk integral makes every in-box point NaN, as (istar - I A)/istar does
-    const float is = A.istar32[(size_t)pv * A.npb + pb];
+    float is;
+    if (A.ld_direct) {
+      float c[ORB_MAX_LDPAR];
+      ld_coefs_f32(A, pv, pb, c);
+      ld_integral<float>(A.law, c, is);
+    } else {
+      is = A.istar32[(size_t)pv * A.npb + pb];
+    }
     float* q = A.lc32 + ((size_t)pv * A.nlc + lc) * LC32;
     q[LC_FLO] = (float)(lo - err);
     q[LC_FHI] = (float)(hi + err);
@@ -342,6 +377,119 @@ __global__ void orbit_kernel(OrbitArgs A) {
   }
   o[14] = __int_as_float(flags);
   o[15] = 0.0f;
+}
+
+template <bool SPLIT>
+__global__ void orbit_kernel(OrbitArgs A) {
+  const int pv = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pv < A.npv) orbit_pv<SPLIT>(A, pv);
+}
+
+// ---------------------------------------------------------------------------
+// Fused split prologue for the affine laws with an analytic disk integral
+// (uniform, linear, quadratic, quadratic-tri): one launch does the work of
+// ld_tables_kernel<float>, ldm_basis_kernel<float> and orbit_kernel<true>
+// (rrmodel.py:212-227 and model_full.py:39-71).
+//   blocks [0, norb): orbit blocks.  Their first warp takes 32 pvs, one per
+//     lane: the FP64 orbit chain is latency-bound, so it is spread thin, and
+//     the lane evaluates the disk integral and the profile's validity probe
+//     itself instead of waiting for the LD tables.
+//   blocks [norb, ...): LD blocks, one warp per pv: the profile on the mu
+//     grid and its disk integral (written out as ld_tables_kernel<float> does),
+//     then the LD means from the basis tables, in FP32 (FP64 only for a pv
+//     whose k lies outside the tables).
+// The orbit blocks come first in the grid, so their chains start at once and
+// the LD blocks fill the SMs around them.
+// ---------------------------------------------------------------------------
+constexpr int PRO_THREADS = 128;
+constexpr int PRO_WARPS = PRO_THREADS / 32;
+constexpr int PRO_MAX_COEF = 128;   // npb * npar and npb * nb floats staged per warp
+
+struct ProArgs {
+  OrbitArgs orb;
+  int npv, npb, npar, nz, nb, nk, ng, law, kw_stride;
+  const double *ldc, *mu, *kw, *ze;
+  double kmin, kmax, dk, inv_dk;
+  const float* B;
+  float *ldp, *istar, *ldm;
+};
+
+// Basis coefficients of one passband from its FP32 coefficients
+// (basis_coefs on the FP32 values).
+__device__ inline void basis_coefs_f32(int law, const float* c, int npar, float* coef) {
+  switch (law) {
+    case LD_QUADRATIC_TRI: {
+      const float a = sqrtf(c[0]), b = 2.0f * c[1];
+      coef[0] = 1.0f; coef[1] = a * b; coef[2] = a * (1.0f - b);
+      return;
+    }
+    default:
+      coef[0] = 1.0f;
+      for (int i = 1; i < basis_count(law, npar); ++i) coef[i] = c[i - 1];
+  }
+}
+
+__global__ void __launch_bounds__(PRO_THREADS) prologue_split_kernel(ProArgs P, int norb) {
+  __shared__ float s_mu[MAX_NZ];
+  __shared__ float s_c[PRO_WARPS][PRO_MAX_COEF];
+  __shared__ float s_coef[PRO_WARPS][PRO_MAX_COEF];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if ((int)blockIdx.x < norb) {
+    if (warp != 0) return;
+    const int pv = blockIdx.x * 32 + lane;
+    if (pv < P.npv) orbit_pv<true>(P.orb, pv);
+    return;
+  }
+  for (int i = threadIdx.x; i < P.nz; i += PRO_THREADS) s_mu[i] = (float)P.mu[i];
+  __syncthreads();
+  const int pv = ((int)blockIdx.x - norb) * PRO_WARPS + warp;
+  if (pv >= P.npv) return;   // warp-uniform; no block barrier follows
+  const int npb = P.npb, npar = P.npar, nz = P.nz, nb = P.nb, ng = P.ng;
+  float* sc = s_c[warp];
+  float* scf = s_coef[warp];
+  for (int i = lane; i < npb * npar; i += 32) sc[i] = (float)P.ldc[(size_t)pv * npb * npar + i];
+  __syncwarp();
+  // the profile and its disk integral (ld_tables_kernel<float>)
+  float* ldp_pv = P.ldp + (size_t)pv * npb * nz;
+  for (int j = lane; j < npb * nz; j += 32) {
+    const int pb = j / nz, z = j - pb * nz;
+    ldp_pv[j] = ld_value<float>(P.law, s_mu[z], sc + pb * npar, npar);
+  }
+  for (int pb = lane; pb < npb; pb += 32) {
+    float is;
+    ld_integral<float>(P.law, sc + pb * npar, is);
+    P.istar[(size_t)pv * npb + pb] = is;
+    basis_coefs_f32(P.law, sc + pb * npar, npar, scf + pb * nb);
+  }
+  __syncwarp();
+  // the LD means (ldm_basis_kernel)
+  float* out = P.ldm + (size_t)pv * npb * ng;
+  const double k = P.kw[(size_t)pv * P.kw_stride];
+  int ik = -1;
+  double ak = 0.0;
+  if (P.kmin <= k && k <= P.kmax) {
+    ik = (int)floor((k - P.kmin) * P.inv_dk);
+    ak = (k - P.kmin - ik * P.dk) * P.inv_dk;
+    if (ik + 1 >= P.nk || ik < 0) ik = -1;
+  }
+  if (ik >= 0) {
+    const float a1 = (float)ak, a0 = 1.0f - a1;
+    const float* B0 = P.B + (size_t)ik * nb * ng;
+    const float* B1 = B0 + (size_t)nb * ng;
+    for (int pb = 0; pb < npb; ++pb) {
+      const float* cf = scf + pb * nb;
+      for (int g = lane; g < ng; g += 32) {
+        float d0 = 0.0f, d1 = 0.0f;
+        for (int b = 0; b < nb; ++b) {
+          d0 += cf[b] * __ldg(B0 + b * ng + g);
+          d1 += cf[b] * __ldg(B1 + b * ng + g);
+        }
+        out[(size_t)pb * ng + g] = a0 * d0 + a1 * d1;
+      }
+    }
+  } else {
+    for (int g = lane; g < ng; g += 32) ldm_direct_g(k, g, ng, nz, P.ze, (const float*)ldp_pv, npb, out);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -828,15 +976,26 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
   }
 }
 
-// Grid: x = ranges of warp tiles, y/z = parameter vectors.
+// Flux launch shape: blocks of FLUX_NW warps, each block one range of at
+// most FLUX_CHUNK consecutive warp tiles of one pv (its warps interleaved over
+// the range).  Grid: x = tile ranges, y/z = parameter vectors.  A small block
+// gives its registers back as soon as its own tiles are done, so a range that
+// holds a transit keeps no finished warps resident, and the hardware block
+// scheduler balances the ranges over the SMs.  The pv's records are staged in
+// dynamic shared memory sized to the light-curve count.
+constexpr int FLUX_NW = 2;
+constexpr int FLUX_CHUNK = 32;
+
 template <bool LC_IN_SMEM>
-__global__ void __launch_bounds__(SPLIT_WARPS * 32) flux_split_kernel(FluxSplitArgs A) {
-  __shared__ WarpList lists[SPLIT_WARPS];
-  __shared__ __align__(16) float recs[ORB32 + (LC_IN_SMEM ? LC_SMEM * LC32 : 0)];
+__global__ void __launch_bounds__(FLUX_NW * 32) flux_split_kernel(FluxSplitArgs A, int chunk) {
+  __shared__ WarpList lists[FLUX_NW];
+  extern __shared__ __align__(16) float flux_recs[];
   const int pv = block_pv();
   if (pv >= A.npv) return;  // block-uniform
   const int ntiles = (A.npt + WARP_TILE - 1) / WARP_TILE;
-  split_pv_tiles(A, pv, blockIdx.x * SPLIT_WARPS, gridDim.x * SPLIT_WARPS, ntiles, recs, LC_IN_SMEM, lists);
+  const int t0 = blockIdx.x * chunk;
+  const int t1 = t0 + chunk < ntiles ? t0 + chunk : ntiles;
+  split_pv_tiles(A, pv, t0, FLUX_NW, t1, flux_recs, LC_IN_SMEM, lists);
 }
 
 // ---------------------------------------------------------------------------
@@ -1016,6 +1175,50 @@ int rr_prepare_split(double t_ref, double t_absmax, const double* k, int nkc, co
   return check_launch("rr_prepare_split");
 }
 
+int rr_prepare_split_ld(double t_ref, double t_absmax, const double* k, int nkc, const double* t0, int ldt0,
+                        int nep, const double* p, const double* a, const double* inc, const double* e,
+                        const double* w, int npv, int nlc, int npb, const int32_t* pbids, const int32_t* epids,
+                        const int32_t* nsamples, const double* exptimes, int law, const double* ldc, int npar,
+                        const double* mu, int nz, const float* basis, int nb, const float* weights, int nk, int ng,
+                        double dk, double kmin, double kmax, const double* z_edges, float* ldp, float* istar,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  const bool analytic = law == LD_UNIFORM || law == LD_LINEAR || law == LD_QUADRATIC || law == LD_QUADRATIC_TRI;
+  const bool fused = analytic && basis && ldc && mu && nb > 0 && nb <= MAX_BASIS && nb == basis_count(law, npar) &&
+                     npar >= 0 && npar <= ORB_MAX_LDPAR && npb * npar <= PRO_MAX_COEF && npb * nb <= PRO_MAX_COEF;
+  if (!fused) {
+    int st = rr_ld_tables_f32(law, ldc, npv, npb, npar, mu, nz, ldp, istar, stream);
+    if (st) return st;
+    return rr_prepare_split(t_ref, t_absmax, k, nkc, t0, ldt0, nep, p, a, inc, e, w, npv, nlc, npb, pbids, epids,
+                            nsamples, exptimes, ldp, istar, weights, nk, ng, nz, dk, kmin, kmax, z_edges, workspace,
+                            workspace_bytes, stream, law, ldc, npar, basis, nb);
+  }
+  if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
+  if (npv < 0 || nlc < 1 || npb < 1 || nk < 2 || ng < 2 || nz < 1 || nz > MAX_NZ || nkc < 1 || nep < 1 ||
+      nep > ldt0 || !ldp || !istar)
+    return RR_ERR_ARG;
+  if (npv == 0) return RR_OK;
+  if (workspace_bytes < rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng)) return RR_ERR_WORKSPACE;
+  SplitTables t = carve_split(workspace, npv, npb, nlc, ng);
+  ProArgs P{};
+  OrbitArgs& oa = P.orb;
+  oa.k = k; oa.t0 = t0; oa.p = p; oa.a = a; oa.inc = inc; oa.e = e; oa.w = w; oa.exptimes = exptimes;
+  oa.pbids = pbids; oa.epids = epids; oa.nsamples = nsamples;
+  oa.nkc = nkc; oa.ldt0 = ldt0; oa.nep = nep; oa.npv = npv; oa.nlc = nlc; oa.npb = npb; oa.nz = nz;
+  oa.ldp = nullptr; oa.ldp_is_f32 = 1; oa.orb32 = t.orb; oa.lc32 = t.lc;
+  oa.istar32 = nullptr; oa.t_ref = t_ref; oa.t_absmax = t_absmax;
+  oa.ld_direct = 1; oa.law = law; oa.npar = npar; oa.ldc = ldc;
+  P.npv = npv; P.npb = npb; P.npar = npar; P.nz = nz; P.nb = nb; P.nk = nk; P.ng = ng; P.law = law;
+  P.kw_stride = nkc; P.ldc = ldc; P.mu = mu; P.kw = k; P.ze = z_edges;
+  P.kmin = kmin; P.kmax = kmax; P.dk = dk; P.inv_dk = 1.0 / dk;
+  P.B = basis; P.ldp = ldp; P.istar = istar; P.ldm = t.ldm;
+  oa.mu = mu;
+  cudaStream_t s = as_stream(stream);
+  const int norb = (npv + 31) / 32;
+  const int nld = (npv + PRO_WARPS - 1) / PRO_WARPS;
+  prologue_split_kernel<<<norb + nld, PRO_THREADS, 0, s>>>(P, norb);
+  return check_launch("rr_prepare_split_ld");
+}
+
 int rr_flux_split(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
                   double dg, const void* workspace, float* flux, int ldflux, void* stream) {
   return rr_flux_split_range(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, 0, npv, flux, ldflux, stream);
@@ -1038,16 +1241,19 @@ int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, in
   npv = pv1 - pv0;
   fa.npt = npt; fa.npv = npv; fa.npb = npb; fa.nlc = nlc; fa.ng = ng; fa.ldflux = ldflux;
   fa.inv_dg = (float)(1.0 / dg); fa.flux = flux;
-  // blocks per pv: enough for about 16 blocks per SM, each warp looping over tiles
+  // tile ranges of FLUX_CHUNK tiles, shorter when the launch would otherwise
+  // have fewer than about four blocks per resident warp slot (152 SMs x 32)
   const int ntiles = (npt + WARP_TILE - 1) / WARP_TILE;
-  const int max_bx = (ntiles + SPLIT_WARPS - 1) / SPLIT_WARPS;
-  long long bx = (152LL * 16 + npv - 1) / npv;
-  bx = bx < 1 ? 1 : (bx > max_bx ? max_bx : bx);
+  long long chunk = (long long)ntiles * npv / (4LL * 152 * 32);
+  chunk = chunk < 1 ? 1 : (chunk > FLUX_CHUNK ? FLUX_CHUNK : chunk);
+  const int bx = (int)((ntiles + chunk - 1) / chunk);
   dim3 fg((unsigned)bx, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
-  if (nlc <= LC_SMEM)
-    flux_split_kernel<true><<<fg, SPLIT_WARPS * 32, 0, as_stream(stream)>>>(fa);
+  const bool lc_smem = nlc <= LC_SMEM;
+  const size_t smem = sizeof(float) * (ORB32 + (lc_smem ? (size_t)nlc * LC32 : 0));
+  if (lc_smem)
+    flux_split_kernel<true><<<fg, FLUX_NW * 32, smem, as_stream(stream)>>>(fa, (int)chunk);
   else
-    flux_split_kernel<false><<<fg, SPLIT_WARPS * 32, 0, as_stream(stream)>>>(fa);
+    flux_split_kernel<false><<<fg, FLUX_NW * 32, smem, as_stream(stream)>>>(fa, (int)chunk);
   return check_launch("rr_flux_split");
 }
 

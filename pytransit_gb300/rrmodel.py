@@ -398,7 +398,6 @@ class RoadRunnerModel(TransitModel):
         split = self.precision == 'split'
         tb = self._device_tables(device)
         dd = self._device_data(device)
-        ldp, istar = self._ld_tables(ldc, npv, npb, device, split, args.get('ldc'))
         L = _lib.lib()
         stream = _lib.stream_ptr(device)
         nz = self.ze.size
@@ -406,6 +405,13 @@ class RoadRunnerModel(TransitModel):
         ldc_d = args.get('ldc')
         npar = int(ldc_d.shape[2]) if ldc_d is not None else 0
         basis, nb = self._basis(device, npar, split) if ldc_d is not None else (None, 0)
+        # a named law in the split path: the LD tables are made by the prologue launch itself
+        fused = split and self.ld_law is not None and ldc_d is not None
+        if fused:
+            ldp = torch.empty((npv, npb, nz), dtype=torch.float32, device=device)
+            istar = torch.empty((npv, npb), dtype=torch.float32, device=device)
+        else:
+            ldp, istar = self._ld_tables(ldc, npv, npb, device, split, ldc_d)
         kmin, kmax = float(self.klims[0]), float(self.klims[1])
         # A pinned host float32 buffer for the split path is filled in pv
         # chunks: chunk c+1 is computed while chunk c is copied to the host.
@@ -418,12 +424,21 @@ class RoadRunnerModel(TransitModel):
             nep = t0.shape[1]
             wsb = L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, self.ng)
             ws = self._workspace(wsb, device)
-            st = L.rr_prepare_split(dd['t_ref'], dd['t_absmax'], P(args['k']), k.shape[1], P(args['t0']),
-                                    t0.shape[1], nep, P(args['p']), P(args['a']), P(args['i']), P(args['e']),
-                                    P(args['w']), npv, nlc, npb, P(dd['pbids']), P(dd['epids']),
-                                    P(dd['nsamples']), P(dd['exptimes']), P(ldp), P(istar), P(tb['W32']), self.nk,
-                                    self.ng, nz, self.dk, kmin, kmax, P(tb['ze']), P(ws), ws.numel(), stream,
-                                    self.ld_law or 0, P(ldc_d), npar, P(basis), nb)
+            if fused:
+                st = L.rr_prepare_split_ld(dd['t_ref'], dd['t_absmax'], P(args['k']), k.shape[1], P(args['t0']),
+                                           t0.shape[1], nep, P(args['p']), P(args['a']), P(args['i']),
+                                           P(args['e']), P(args['w']), npv, nlc, npb, P(dd['pbids']),
+                                           P(dd['epids']), P(dd['nsamples']), P(dd['exptimes']), self.ld_law,
+                                           P(ldc_d), npar, P(tb['mu']), nz, P(basis), nb, P(tb['W32']), self.nk,
+                                           self.ng, self.dk, kmin, kmax, P(tb['ze']), P(ldp), P(istar), P(ws),
+                                           ws.numel(), stream)
+            else:
+                st = L.rr_prepare_split(dd['t_ref'], dd['t_absmax'], P(args['k']), k.shape[1], P(args['t0']),
+                                        t0.shape[1], nep, P(args['p']), P(args['a']), P(args['i']), P(args['e']),
+                                        P(args['w']), npv, nlc, npb, P(dd['pbids']), P(dd['epids']),
+                                        P(dd['nsamples']), P(dd['exptimes']), P(ldp), P(istar), P(tb['W32']),
+                                        self.nk, self.ng, nz, self.dk, kmin, kmax, P(tb['ze']), P(ws), ws.numel(),
+                                        stream, self.ld_law or 0, P(ldc_d), npar, P(basis), nb)
             if st == 0 and pipe:
                 st = self._flux_to_host(dd, npt, npv, nlc, npb, ws, user_out.view(npv, npt), device)
             elif st == 0:
