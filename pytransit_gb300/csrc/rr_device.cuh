@@ -387,6 +387,43 @@ __device__ inline void solve2d_conj(double p, double a, double inc, double e, do
   c[5] = -ci * P0y; c[6] = -ci * P1y; c[7] = -ci * P2y; c[8] = -ci * P3y; c[9] = -ci * P4y;
 }
 
+// solve2d_conj in FP32 for the split path, whose flux kernel reads the
+// coefficients as FP32 anyway.  Each coefficient carries a few FP32 roundings
+// more than the FP64 jet rounded once (relative error ~1e-7, |dz| ~1e-7 near
+// transit), and the FP64 pipe, 1/64 of the FP32 rate on this GPU, drops out
+// of the prologue's serial chain.  cos i is taken as sin(pi/2 - i) of the
+// small angle pi/2 - i formed in FP64, so that b = a cos i keeps its relative
+// precision for near-edge-on orbits with large a; sin w and cos w only enter
+// multiplied by e.
+__device__ inline void solve2d_conj_f32(double p, double a, double inc, double e, double w, float* c) {
+  const float af = (float)a, ef = (float)e;
+  const float n = (float)(2.0 * PI) / (float)p;
+  const float se = sqrtf(1.0f - ef * ef);
+  float sf = 1.0f, cf = 0.0f;   // f = pi/2 - w: sin f = cos w, cos f = sin w
+  if (ef != 0.0f) sincosf((float)w, &cf, &sf);
+  const float r = af * (1.0f - ef * ef) / (1.0f + ef * cf);
+  const float vr = n * af * ef * sf / se;
+  const float vt = n * af * (1.0f + ef * cf) / se;
+  const float P0x = 0.0f, P0y = r;
+  const float P1x = -vt, P1y = vr;
+  const float mu = n * n * af * af * af;
+  const float alpha = -1.5f;
+  const float q0 = P0x * P0x + P0y * P0y;
+  const float q1 = 2.0f * (P0x * P1x + P0y * P1y);
+  const float s0 = 1.0f / (q0 * sqrtf(q0));
+  const float P2x = -mu * s0 * P0x / 2.0f, P2y = -mu * s0 * P0y / 2.0f;
+  const float s1 = alpha * q1 * s0 / q0;
+  const float P3x = -mu * (s0 * P1x + s1 * P0x) / 6.0f;
+  const float P3y = -mu * (s0 * P1y + s1 * P0y) / 6.0f;
+  const float q2 = 2.0f * (P0x * P2x + P0y * P2y) + (P1x * P1x + P1y * P1y);
+  const float s2 = ((alpha - 1.0f) * q1 * s1 + 2.0f * alpha * q2 * s0) / (2.0f * q0);
+  const float P4x = -mu * (s0 * P2x + s1 * P1x + s2 * P0x) / 12.0f;
+  const float P4y = -mu * (s0 * P2y + s1 * P1y + s2 * P0y) / 12.0f;
+  const float ci = sinf((float)(0.5 * PI - inc));
+  c[0] = -P0x; c[1] = -P1x; c[2] = -P2x; c[3] = -P3x; c[4] = -P4x;
+  c[5] = -ci * P0y; c[6] = -ci * P1y; c[7] = -ci * P2y; c[8] = -ci * P3y; c[9] = -ci * P4y;
+}
+
 __device__ inline double sep_c_f64(double t, const double* c) {
   double x = c[0] + t * (c[1] + t * (c[2] + t * (c[3] + t * c[4])));
   double y = c[5] + t * (c[6] + t * (c[7] + t * (c[8] + t * c[9])));
@@ -466,6 +503,50 @@ __device__ inline float contact_point_f32(float k, int point, const float* c) {
     }
   }
   return t1;
+}
+
+// Points 1 and 4 of contact_point_f32 (the outer contacts) bisected in one
+// loop: each keeps its own bracket and stops on its own test, so the results
+// are those of the two separate calls, while the two dependent chains overlap.
+__device__ inline void contact_points14_f32(float k, const float* c, float& t1, float& t4) {
+  const float zt = 1.0f + k;
+  float a0 = 0.0f, a2 = -2.0f / fabsf(c[1]);
+  float a1 = 0.5f * a2;
+  float b0 = 0.0f, b2 = 2.0f / fabsf(c[1]);
+  float b1 = 0.5f * b2;
+  const float z00 = sep_c_f32(0.0f, c) - zt;
+  float za0 = z00, za1 = sep_c_f32(a1, c) - zt;
+  float zb0 = z00, zb1 = sep_c_f32(b1, c) - zt;
+  bool ra = true, rb = true;
+  for (int i = 0; i < 100; ++i) {
+    ra = ra && fabsf(a2 - a0) > 1e-6f;
+    rb = rb && fabsf(b2 - b0) > 1e-6f;
+    if (!ra && !rb) break;
+    if (ra) {
+      if (za0 * za1 < 0.0f) {
+        a2 = a1;
+        a1 = 0.5f * (a0 + a1);
+      } else {
+        a0 = a1;
+        a1 = 0.5f * (a1 + a2);
+        za0 = za1;
+      }
+      za1 = sep_c_f32(a1, c) - zt;
+    }
+    if (rb) {
+      if (zb0 * zb1 < 0.0f) {
+        b2 = b1;
+        b1 = 0.5f * (b0 + b1);
+      } else {
+        b0 = b1;
+        b1 = 0.5f * (b1 + b2);
+        zb0 = zb1;
+      }
+      zb1 = sep_c_f32(b1, c) - zt;
+    }
+  }
+  t1 = a1;
+  t4 = b1;
 }
 
 }  // namespace rr

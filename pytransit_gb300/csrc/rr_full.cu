@@ -289,94 +289,125 @@ __device__ inline void ld_coefs_f32(const OrbitArgs& A, int pv, int pb, float* c
   for (int i = 0; i < ORB_MAX_LDPAR; ++i) c[i] = i < A.npar ? (float)src[i] : 0.0f;
 }
 
-template <bool SPLIT>
-__device__ __forceinline__ void orbit_pv(const OrbitArgs& A, int pv) {
-  double a = A.a[pv], e = A.e[pv], p = A.p[pv];
+// Plain FP64 path: validity, the FP64 Taylor coefficients and the contact
+// times of one pv.
+__device__ __forceinline__ void orbit_pv_f64(const OrbitArgs& A, int pv) {
+  const double a = A.a[pv], e = A.e[pv], p = A.p[pv];
+  const bool ldbad = A.ldp_is_f32 ? isnan(((const float*)A.ldp)[(size_t)pv * A.npb * A.nz])
+                                  : isnan(((const double*)A.ldp)[(size_t)pv * A.npb * A.nz]);
+  const bool valid = !(isnan(a) || a <= 1.0 || e < 0.0 || ldbad);
+  double c[10];
+  double t1 = 0.0, t4 = 0.0;
+  const double k0 = A.k[(size_t)pv * A.nkc];
+  if (valid) {
+    solve2d_conj(p, a, A.inc[pv], e, A.w[pv], c);
+    t1 = contact_point(k0, 1, c);
+    t4 = contact_point(k0, 4, c);
+  } else {
+    for (int i = 0; i < 10; ++i) c[i] = 0.0;
+  }
+  double* o = A.orb64 + (size_t)pv * ORB64;
+  for (int i = 0; i < 10; ++i) o[i] = c[i];
+  o[10] = t1;
+  o[11] = t4;
+  o[12] = valid ? 1.0 : 0.0;
+}
+
+// Split path: the FP32 orbit record [ORB32] and the per-light-curve records
+// [nlc][LC32] of one pv.  The pointers are restrict-qualified locals and the
+// light curves go in groups of four with every load of a group issued before
+// its records are stored, so the dependent loads (epoch id -> zero epoch,
+// passband id -> coefficients) of different light curves overlap; both
+// contact points are bisected in one loop; records are written 16 bytes at a
+// time.
+constexpr int ORB_LCG = 2;   // light curves per load group
+
+__device__ __forceinline__ void orbit_pv_split(const OrbitArgs& A, int pv) {
+  const double* __restrict__ t0v = A.t0 + (size_t)pv * A.ldt0;
+  const double* __restrict__ kv = A.k + (size_t)pv * A.nkc;
+  const double* __restrict__ exptimes = A.exptimes;
+  const int32_t* __restrict__ epids = A.epids;
+  const int32_t* __restrict__ pbids = A.pbids;
+  const int32_t* __restrict__ nsamples = A.nsamples;
+  float4* __restrict__ o4 = reinterpret_cast<float4*>(A.orb32 + (size_t)pv * ORB32);
+  float4* __restrict__ q4 = reinterpret_cast<float4*>(A.lc32 + (size_t)pv * A.nlc * LC32);
+  const double a = A.a[pv], e = A.e[pv], p = A.p[pv], inc = A.inc[pv], w = A.w[pv];
+  const double k0 = kv[0];
   bool ldbad;
-  if (SPLIT && A.ld_direct) {
+  if (A.ld_direct) {
     float c[ORB_MAX_LDPAR];
     ld_coefs_f32(A, pv, 0, c);
     ldbad = isnan(ld_value<float>(A.law, (float)A.mu[0], c, A.npar));
   } else {
-    ldbad = A.ldp_is_f32 ? isnan(((const float*)A.ldp)[(size_t)pv * A.npb * A.nz])
-                         : isnan(((const double*)A.ldp)[(size_t)pv * A.npb * A.nz]);
+    ldbad = isnan(((const float*)A.ldp)[(size_t)pv * A.npb * A.nz]);
   }
-  bool valid = !(isnan(a) || a <= 1.0 || e < 0.0 || ldbad);
-  double c[10];
-  float cf[10];
-  double t1 = 0.0, t4 = 0.0;
-  double k0 = A.k[(size_t)pv * A.nkc];
-  if (valid) {
-    solve2d_conj(p, a, A.inc[pv], e, A.w[pv], c);
-    for (int i = 0; i < 10; ++i) cf[i] = (float)c[i];
-    if (SPLIT) {
-      t1 = contact_point_f32((float)k0, 1, cf);
-      t4 = contact_point_f32((float)k0, 4, cf);
-    } else {
-      t1 = contact_point(k0, 1, c);
-      t4 = contact_point(k0, 4, c);
-    }
-  } else {
-    for (int i = 0; i < 10; ++i) { c[i] = 0.0; cf[i] = 0.0f; }
-  }
-  if (!SPLIT) {
-    double* o = A.orb64 + (size_t)pv * ORB64;
-    for (int i = 0; i < 10; ++i) o[i] = c[i];
-    o[10] = t1;
-    o[11] = t4;
-    o[12] = valid ? 1.0 : 0.0;
-    return;
-  }
-  float* o = A.orb32 + (size_t)pv * ORB32;
-  for (int i = 0; i < 10; ++i) o[i] = cf[i];
-  float p_hi = __double2float_rn(p);
-  float p_lo = __double2float_rn(p - (double)p_hi);
-  o[10] = p_hi;
-  o[11] = p_lo;
-  o[12] = __double2float_rn(1.0 / p);
   double d0max = 0.0;
-  for (int ep = 0; ep < A.nep; ++ep) d0max = fmax(d0max, fabs(A.t0[(size_t)pv * A.ldt0 + ep] - A.t_ref));
+  for (int ep = 0; ep < A.nep; ++ep) d0max = fmax(d0max, fabs(t0v[ep] - A.t_ref));
+  const bool valid = !(isnan(a) || a <= 1.0 || e < 0.0 || ldbad);
+  float cf[10];
+  float t1 = 0.0f, t4 = 0.0f;
+  if (valid) {
+    solve2d_conj_f32(p, a, inc, e, w, cf);
+    contact_points14_f32((float)k0, cf, t1, t4);
+  } else {
+    for (int i = 0; i < 10; ++i) cf[i] = 0.0f;
+  }
+  const float p_hi = __double2float_rn(p);
+  const float p_lo = __double2float_rn(p - (double)p_hi);
   // Bound of |fast-test tc - true tc|: 2^-24 (4 (T + |d0|) + 2 p), doubled.
   const double err = ldexp(1.0, -21) * (A.t_absmax + d0max + p) + 1e-9;
-  o[13] = (float)err;
   int flags = valid ? FLAG_VALID : 0;
-  for (int lc = 0; lc < A.nlc; ++lc) {
-    const double pad = 0.003 + A.exptimes[lc];
-    const double lo = t1 - pad, hi = t4 + pad;
-    if (hi + 2 * err >= 0.5 * p || lo - 2 * err <= -0.5 * p) flags |= FLAG_WIDE;
-    const int ep = A.epids[lc];
-    const int pb = A.pbids[lc];
-    const int ns = A.nsamples[lc];
-    const double d0 = A.t0[(size_t)pv * A.ldt0 + ep] - A.t_ref;
-    const float d0h = __double2float_rn(d0);
-    const double kk = A.k[(size_t)pv * A.nkc + (A.nkc == A.npb ? pb : 0)];
-    // a non-finite disk integral makes every in-box point NaN, as (istar - I A)/istar does
-    float is;
-    if (A.ld_direct) {
-      float c[ORB_MAX_LDPAR];
-      ld_coefs_f32(A, pv, pb, c);
-      ld_integral<float>(A.law, c, is);
-    } else {
-      is = A.istar32[(size_t)pv * A.npb + pb];
+  for (int lc0 = 0; lc0 < A.nlc; lc0 += ORB_LCG) {
+    double d0[ORB_LCG], kk[ORB_LCG], ex[ORB_LCG];
+    int pb[ORB_LCG], ns[ORB_LCG];
+    float is[ORB_LCG];
+#pragma unroll
+    for (int j = 0; j < ORB_LCG; ++j) {
+      const int lc = min(lc0 + j, A.nlc - 1);
+      pb[j] = pbids[lc];
+      ns[j] = nsamples[lc];
+      ex[j] = exptimes[lc];
+      d0[j] = t0v[epids[lc]] - A.t_ref;
+      kk[j] = kv[A.nkc == A.npb ? pb[j] : 0];
+      // a non-finite disk integral makes every in-box point NaN, as (istar - I A)/istar does
+      if (A.ld_direct) {
+        float c[ORB_MAX_LDPAR];
+        ld_coefs_f32(A, pv, pb[j], c);
+        ld_integral<float>(A.law, c, is[j]);
+      } else {
+        is[j] = A.istar32[(size_t)pv * A.npb + pb[j]];
+      }
     }
-    float* q = A.lc32 + ((size_t)pv * A.nlc + lc) * LC32;
-    q[LC_FLO] = (float)(lo - err);
-    q[LC_FHI] = (float)(hi + err);
-    q[LC_D0H] = d0h;
-    q[LC_D0L] = __double2float_rn(d0 - (double)d0h);
-    q[LC_LO] = (float)lo;
-    q[LC_HI] = (float)hi;
-    q[LC_K] = (float)kk;
-    q[LC_INV1PK] = (float)(1.0 / (1.0 + kk));
-    q[LC_INVIS] = isfinite(is) ? 1.0f / is : __int_as_float(0x7fc00000);
-    q[LC_EXPT] = (float)A.exptimes[lc];
-    q[LC_INVNS] = 1.0f / (float)ns;
-    q[LC_NS] = __int_as_float(ns);
-    q[LC_PB] = __int_as_float(pb);
-    q[13] = q[14] = q[15] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < ORB_LCG; ++j) {
+      const int lc = lc0 + j;
+      if (lc >= A.nlc) break;
+      const double pad = 0.003 + ex[j];
+      const double lo = (double)t1 - pad, hi = (double)t4 + pad;
+      if (hi + 2 * err >= 0.5 * p || lo - 2 * err <= -0.5 * p) flags |= FLAG_WIDE;
+      const float d0h = __double2float_rn(d0[j]);
+      const float kf = (float)kk[j];
+      float4* q = q4 + (size_t)lc * (LC32 / 4);
+      // LC_FLO, LC_FHI, LC_D0H, LC_D0L | LC_LO, LC_HI, LC_K, LC_INV1PK | LC_INVIS, LC_EXPT, LC_INVNS, LC_NS | LC_PB
+      q[0] = make_float4((float)(lo - err), (float)(hi + err), d0h, __double2float_rn(d0[j] - (double)d0h));
+      q[1] = make_float4((float)lo, (float)hi, kf, 1.0f / (1.0f + kf));
+      q[2] = make_float4(isfinite(is[j]) ? 1.0f / is[j] : __int_as_float(0x7fc00000), (float)ex[j],
+                         1.0f / (float)ns[j], __int_as_float(ns[j]));
+      q[3] = make_float4(__int_as_float(pb[j]), 0.0f, 0.0f, 0.0f);
+    }
   }
-  o[14] = __int_as_float(flags);
-  o[15] = 0.0f;
+  o4[0] = make_float4(cf[0], cf[1], cf[2], cf[3]);
+  o4[1] = make_float4(cf[4], cf[5], cf[6], cf[7]);
+  o4[2] = make_float4(cf[8], cf[9], p_hi, p_lo);
+  o4[3] = make_float4(1.0f / p_hi, (float)err, __int_as_float(flags), 0.0f);
+}
+
+template <bool SPLIT>
+__device__ __forceinline__ void orbit_pv(const OrbitArgs& A, int pv) {
+  if (SPLIT)
+    orbit_pv_split(A, pv);
+  else
+    orbit_pv_f64(A, pv);
 }
 
 template <bool SPLIT>
@@ -429,7 +460,9 @@ __device__ inline void basis_coefs_f32(int law, const float* c, int npar, float*
   }
 }
 
-__global__ void __launch_bounds__(PRO_THREADS) prologue_split_kernel(ProArgs P, int norb) {
+template <int LAW>
+__global__ void __launch_bounds__(PRO_THREADS, 8) prologue_split_kernel(ProArgs P, int norb) {
+  constexpr int NB = LAW == LD_UNIFORM ? 1 : (LAW == LD_LINEAR ? 2 : 3);   // basis_count of the law
   __shared__ float s_mu[MAX_NZ];
   __shared__ float s_c[PRO_WARPS][PRO_MAX_COEF];
   __shared__ float s_coef[PRO_WARPS][PRO_MAX_COEF];
@@ -444,47 +477,49 @@ __global__ void __launch_bounds__(PRO_THREADS) prologue_split_kernel(ProArgs P, 
   __syncthreads();
   const int pv = ((int)blockIdx.x - norb) * PRO_WARPS + warp;
   if (pv >= P.npv) return;   // warp-uniform; no block barrier follows
-  const int npb = P.npb, npar = P.npar, nz = P.nz, nb = P.nb, ng = P.ng;
+  const int npb = P.npb, npar = P.npar, nz = P.nz, ng = P.ng;
   float* sc = s_c[warp];
   float* scf = s_coef[warp];
   for (int i = lane; i < npb * npar; i += 32) sc[i] = (float)P.ldc[(size_t)pv * npb * npar + i];
   __syncwarp();
-  // the profile and its disk integral (ld_tables_kernel<float>)
+  // the profile and its disk integral (ld_tables_kernel<float>), lanes over the mu grid
   float* ldp_pv = P.ldp + (size_t)pv * npb * nz;
-  for (int j = lane; j < npb * nz; j += 32) {
-    const int pb = j / nz, z = j - pb * nz;
-    ldp_pv[j] = ld_value<float>(P.law, s_mu[z], sc + pb * npar, npar);
-  }
+  for (int pb = 0; pb < npb; ++pb)
+    for (int z = lane; z < nz; z += 32) ldp_pv[pb * nz + z] = ld_value<float>(LAW, s_mu[z], sc + pb * npar, npar);
   for (int pb = lane; pb < npb; pb += 32) {
     float is;
-    ld_integral<float>(P.law, sc + pb * npar, is);
+    ld_integral<float>(LAW, sc + pb * npar, is);
     P.istar[(size_t)pv * npb + pb] = is;
-    basis_coefs_f32(P.law, sc + pb * npar, npar, scf + pb * nb);
+    basis_coefs_f32(LAW, sc + pb * npar, npar, scf + pb * NB);
   }
   __syncwarp();
-  // the LD means (ldm_basis_kernel)
+  // the LD means (ldm_basis_kernel): per grid column g the two k rows' basis
+  // columns are blended once, e_b = (1 - ak) B[ik][b][g] + ak B[ik+1][b][g],
+  // then each passband is an NB-term dot product with its coefficients
   float* out = P.ldm + (size_t)pv * npb * ng;
   const double k = P.kw[(size_t)pv * P.kw_stride];
   int ik = -1;
-  double ak = 0.0;
+  float a1 = 0.0f;
   if (P.kmin <= k && k <= P.kmax) {
-    ik = (int)floor((k - P.kmin) * P.inv_dk);
-    ak = (k - P.kmin - ik * P.dk) * P.inv_dk;
+    const double t = (k - P.kmin) * P.inv_dk;
+    const double fl = floor(t);
+    ik = (int)fl;
+    a1 = (float)(t - fl);
     if (ik + 1 >= P.nk || ik < 0) ik = -1;
   }
   if (ik >= 0) {
-    const float a1 = (float)ak, a0 = 1.0f - a1;
-    const float* B0 = P.B + (size_t)ik * nb * ng;
-    const float* B1 = B0 + (size_t)nb * ng;
-    for (int pb = 0; pb < npb; ++pb) {
-      const float* cf = scf + pb * nb;
-      for (int g = lane; g < ng; g += 32) {
-        float d0 = 0.0f, d1 = 0.0f;
-        for (int b = 0; b < nb; ++b) {
-          d0 += cf[b] * __ldg(B0 + b * ng + g);
-          d1 += cf[b] * __ldg(B1 + b * ng + g);
-        }
-        out[(size_t)pb * ng + g] = a0 * d0 + a1 * d1;
+    const float a0 = 1.0f - a1;
+    const float* B0 = P.B + (size_t)ik * NB * ng;
+    const float* B1 = B0 + (size_t)NB * ng;
+    for (int g = lane; g < ng; g += 32) {
+      float eb[NB];
+#pragma unroll
+      for (int b = 0; b < NB; ++b) eb[b] = a0 * __ldg(B0 + b * ng + g) + a1 * __ldg(B1 + b * ng + g);
+      for (int pb = 0; pb < npb; ++pb) {
+        float d = 0.0f;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) d = fmaf(scf[pb * NB + b], eb[b], d);
+        out[(size_t)pb * ng + g] = d;
       }
     }
   } else {
@@ -1215,7 +1250,12 @@ int rr_prepare_split_ld(double t_ref, double t_absmax, const double* k, int nkc,
   cudaStream_t s = as_stream(stream);
   const int norb = (npv + 31) / 32;
   const int nld = (npv + PRO_WARPS - 1) / PRO_WARPS;
-  prologue_split_kernel<<<norb + nld, PRO_THREADS, 0, s>>>(P, norb);
+  switch (law) {
+    case LD_UNIFORM: prologue_split_kernel<LD_UNIFORM><<<norb + nld, PRO_THREADS, 0, s>>>(P, norb); break;
+    case LD_LINEAR: prologue_split_kernel<LD_LINEAR><<<norb + nld, PRO_THREADS, 0, s>>>(P, norb); break;
+    case LD_QUADRATIC: prologue_split_kernel<LD_QUADRATIC><<<norb + nld, PRO_THREADS, 0, s>>>(P, norb); break;
+    default: prologue_split_kernel<LD_QUADRATIC_TRI><<<norb + nld, PRO_THREADS, 0, s>>>(P, norb); break;
+  }
   return check_launch("rr_prepare_split_ld");
 }
 
