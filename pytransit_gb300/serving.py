@@ -589,16 +589,16 @@ class GpuExecutor:
                 P['flux'] = fl.data_ptr()
             buf[:n_in].copy_(stage[lo:lo + n_in], non_blocking=True)
             self._lib.check(L.rr_time_split(P['time'], P['lcids'], npt, t_ref, P['times_ff'], sp))
-            self._lib.check(L.rr_ld_tables_f32(m.ld_law, P['ldc'], npv, npb, npar, tb['mu_ptr'], nz, P['ldp'],
-                                               P['istar'], sp))
             g = dict(P=P, t_ref=t_ref, t_abs=t_abs, wsb=wsb, block=(blk, total))
             if req.kind == 'rr':
+                # LD tables, LD means and orbit records in one launch
                 basis, nb = m._basis(self.device, npar, True)
-                self._lib.check(L.rr_prepare_split(
+                self._lib.check(L.rr_prepare_split_ld(
                     t_ref, t_abs, P['k'], h['k'].shape[1], P['t0'], nep, nep, P['p'], P['a'], P['i'], P['e'],
-                    P['w'], npv, nlc, npb, P['pbids'], P['epids'], P['nsamples'], P['exptimes'], P['ldp'],
-                    P['istar'], tb['W32_ptr'], m.nk, ng, nz, m.dk, m.klims[0], m.klims[1], tb['ze_ptr'], P['ws'],
-                    wsb, sp, m.ld_law, P['ldc'], npar, None if basis is None else basis.data_ptr(), nb))
+                    P['w'], npv, nlc, npb, P['pbids'], P['epids'], P['nsamples'], P['exptimes'], m.ld_law,
+                    P['ldc'], npar, tb['mu_ptr'], nz, None if basis is None else basis.data_ptr(), nb,
+                    tb['W32_ptr'], m.nk, ng, m.dk, m.klims[0], m.klims[1], tb['ze_ptr'], P['ldp'], P['istar'],
+                    P['ws'], wsb, sp))
                 g['flux'] = (fl if own_flux else buf[off['flux']:off['flux'] + 4 * npv * ldf].view(torch.float32)
                              ).view(npv, ldf)
                 orb, lc, ldm = C.c_void_p(), C.c_void_p(), C.c_void_p()
@@ -613,6 +613,8 @@ class GpuExecutor:
                 d['inv_dg'] = np.float32(1.0 / m.dg)
                 self._dirty.add(slot)
             else:
+                self._lib.check(L.rr_ld_tables_f32(m.ld_law, P['ldc'], npv, npb, npar, tb['mu_ptr'], nz, P['ldp'],
+                                                   P['istar'], sp))
                 g['chunk'] = chunk
                 if self.result == 'device':
                     n = 4 * npv * npb * ldf
