@@ -704,11 +704,22 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
     }
   }
   if (!__ballot_sync(FULL, inb != 0)) return;
-  bool single = true;
+  // Slot q of the lanes holds the tile's 32 consecutive points q*32 .. q*32+31:
+  // a slot without an in-box point skips the per-point work as a whole warp.
+  unsigned act = 0;
 #pragma unroll
-  for (int q = 0; q < SPLIT_PTS; ++q)
-    if (inb >> q & 1u) single = single && (__float_as_int(LCR[lcv[q] * LC32 + LC_NS]) == 1);
-  if (__all_sync(FULL, single)) {
+  for (int q = 0; q < SPLIT_PTS; ++q) act |= (__ballot_sync(FULL, inb >> q & 1u) ? 1u : 0u) << q;
+  bool single;
+  if (tlc >= 0) {
+    single = __float_as_int(RT[LC_NS]) == 1;   // one light curve: warp-uniform
+  } else {
+    single = true;
+#pragma unroll
+    for (int q = 0; q < SPLIT_PTS; ++q)
+      if (inb >> q & 1u) single = single && (__float_as_int(LCR[lcv[q] * LC32 + LC_NS]) == 1);
+    single = __all_sync(FULL, single);
+  }
+  if (single) {
     // One sample per point.  A point whose planet disk is fully inside the
     // star (area pi k^2) is finished in place; points on the limb (kite area,
     // two atan2) are gathered into the warp's list and evaluated 32 at a time,
@@ -725,11 +736,14 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
       const float4 ca = *reinterpret_cast<const float4*>(orb);
       const float4 cb = *reinterpret_cast<const float4*>(orb + 4);
       const float2 cc = *reinterpret_cast<const float2*>(orb + 8);
-      // the four points side by side, without branches until the loads are
-      // issued, so that their dependent chains overlap
+      // the active slots side by side, without per-lane branches until the
+      // loads are issued, so that their dependent chains overlap
       float frq[SPLIT_PTS], l0q[SPLIT_PTS], l1q[SPLIT_PTS];
 #pragma unroll
       for (int q = 0; q < SPLIT_PTS; ++q) {
+        zq[q] = 0.0f;
+        frq[q] = l0q[q] = l1q[q] = 0.0f;
+        if (!(act >> q & 1u)) continue;   // warp-uniform
         const float t = tcq[q];
         const float x = fmaf(t, fmaf(t, fmaf(t, fmaf(t, cb.x, ca.w), ca.z), ca.y), ca.x);
         const float y = fmaf(t, fmaf(t, fmaf(t, fmaf(t, cc.y, cc.x), cb.w), cb.z), cb.y);
@@ -738,12 +752,13 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
         const float gg = fminf(zq[q], lim_out) * gsc;
         const int i = min(max((int)gg, 0), ng - 2);
         frq[q] = gg - (float)i;
-        const bool need = (inb >> q & 1u) && zq[q] <= lim_in;
+        const bool need = (inb >> q & 1u) && zq[q] < lim_out;   // inner and limb points
         l0q[q] = need ? __ldg(lda + i) : 0.0f;
         l1q[q] = need ? __ldg(lda + i + 1) : 0.0f;
       }
 #pragma unroll
       for (int q = 0; q < SPLIT_PTS; ++q) {
+        if (!(act >> q & 1u)) continue;   // warp-uniform
         if (!(inb >> q & 1u)) {
           zq[q] = 0.0f;
         } else if (!(zq[q] < lim_out)) {
@@ -754,6 +769,20 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
           limb |= 1u << q;
         }
       }
+      // Limb points (kite area, two atan2) in place, slot by slot: the limb
+      // points of a slot are consecutive in time (an ingress or an egress),
+      // so one or two slots of a tile hold them all, and their table values
+      // came with the loads above.
+#pragma unroll
+      for (int q = 0; q < SPLIT_PTS; ++q) {
+        if (!(act >> q & 1u)) continue;                    // warp-uniform
+        if (!__ballot_sync(FULL, limb >> q & 1u)) continue;  // warp-uniform
+        if (limb >> q & 1u) {
+          float kap;
+          res[q] = 1.0f - (fmaf(frq[q], l1q[q] - l0q[q], l0q[q]) * ccia_star<float>(k, zq[q], kap)) * invis;
+        }
+      }
+      return;
     } else {
 #pragma unroll
       for (int q = 0; q < SPLIT_PTS; ++q) {
@@ -785,9 +814,10 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
     int posq[SPLIT_PTS];
 #pragma unroll
     for (int q = 0; q < SPLIT_PTS; ++q) {
+      posq[q] = -1;
+      if (!(act >> q & 1u)) continue;   // warp-uniform
       const bool in = limb >> q & 1u;
       const unsigned m = __ballot_sync(FULL, in);
-      posq[q] = -1;
       if (in) {
         const int pos = nl + __popc(m & ((1u << lane) - 1u));
         L.tc[pos] = zq[q];
@@ -932,14 +962,23 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
                                                        time_meta_offset(A.npt));
   WarpList& L = lists[warp];
   const unsigned FULL = 0xffffffffu;
-  for (int j0 = 0; t_first + warp + j0 * t_step < t_end; j0 += 32) {
+  // The warp's tiles are t_first + warp + j t_step, j < ntl.  A culled tile is
+  // one 16-byte store of the fill value per lane (ones; NaN for an invalid
+  // pv, whose tiles are all "culled"); only the row's last tile can be
+  // partial, and it is stored point by point.
+  const int tw0 = t_first + warp;
+  const int ntl = tw0 < t_end ? (t_end - tw0 + t_step - 1) / t_step : 0;
+  const int tile_part = (A.npt % WARP_TILE) ? A.npt / WARP_TILE : -1;
+  const float fill = valid ? 1.0f : __int_as_float(0x7fc00000);
+  const float4 fill4 = make_float4(fill, fill, fill, fill);
+  for (int j0 = 0; j0 < ntl; j0 += 32) {
     // The cull test of the warp's next 32 tiles, one tile per lane: the
     // tile's time range (from its summary) against the box copies around it,
     // the rounding of t - d0 and of j p covered by the error bound in the box
-    // (flo, fhi).  A culled tile is then only a store of ones.
-    const int tl = t_first + warp + (j0 + lane) * t_step;
-    bool cull = false;
-    if (valid && !wide && tl < t_end) {
+    // (flo, fhi).
+    const int tl = tw0 + (j0 + lane) * t_step;
+    bool cull = !valid;
+    if (valid && !wide && j0 + lane < ntl) {
       const float4 tm = __ldg(meta + tl);
       const int tlc = __float_as_int(tm.z);
       if (tlc >= 0) {
@@ -955,58 +994,42 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
         cull = !hit;
       }
     }
-    const unsigned cmask = __ballot_sync(FULL, cull);
-    for (int jt = 0; jt < 32; ++jt) {
-      const int tile = t_first + warp + (j0 + jt) * t_step;
-      if (tile >= t_end) break;
-      const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
-      const bool full4 = pt0 + SPLIT_PTS <= A.npt;
-      if (cmask >> jt & 1u) {
-        if (full4 && row_vec) {
-          __stcs(reinterpret_cast<float4*>(row + pt0), make_float4(1.0f, 1.0f, 1.0f, 1.0f));
+    unsigned cmask = __ballot_sync(FULL, cull);
+    const int jn = min(32, ntl - j0);
+    int tile = tw0 + j0 * t_step;
+    for (int jt = 0; jt < jn; ++jt, tile += t_step, cmask >>= 1) {
+      if (cmask & 1u) {
+        if (row_vec && tile != tile_part) {
+          __stcs(reinterpret_cast<float4*>(row) + (size_t)tile * (WARP_TILE / 4) + lane, fill4);
         } else {
+          const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
           for (int q = 0; q < SPLIT_PTS; ++q)
-            if (pt0 + q < A.npt) __stcs(row + pt0 + q, 1.0f);
+            if (pt0 + q < A.npt) __stcs(row + pt0 + q, fill);
         }
         continue;
       }
+      // The tile reaches a box copy (the cull test above said so).  Slot q of
+      // lane l holds point tile * 128 + q * 32 + l: each slot is 32
+      // consecutive points, coalesced in its loads and stores.
+      const float4 tm = __ldg(meta + tile);                 // tmin, tmax, lc
+      const int ps0 = tile * WARP_TILE + lane;
       float res[SPLIT_PTS] = {1.0f, 1.0f, 1.0f, 1.0f};
-      if (!valid) {
+      float hi[SPLIT_PTS], lo[SPLIT_PTS];
+      int lcv[SPLIT_PTS];
 #pragma unroll
-        for (int q = 0; q < SPLIT_PTS; ++q) res[q] = __int_as_float(0x7fc00000);
-      } else {
-        // the tile reaches a box copy (the cull test above said so)
-        const float4 tm = __ldg(meta + tile);                 // tmin, tmax, lc
-        float hi[SPLIT_PTS], lo[SPLIT_PTS];
-        int lcv[SPLIT_PTS];
-        if (full4 && ((reinterpret_cast<uintptr_t>(A.times_ff + pt0) & 15) == 0) &&
-            ((reinterpret_cast<uintptr_t>(A.lcids + pt0) & 15) == 0)) {
-          const float4 u = __ldg(reinterpret_cast<const float4*>(A.times_ff + pt0));
-          const float4 v = __ldg(reinterpret_cast<const float4*>(A.times_ff + pt0 + 2));
-          const int4 l4 = __ldg(reinterpret_cast<const int4*>(A.lcids + pt0));
-          hi[0] = u.x; lo[0] = u.y; hi[1] = u.z; lo[1] = u.w;
-          hi[2] = v.x; lo[2] = v.y; hi[3] = v.z; lo[3] = v.w;
-          lcv[0] = l4.x; lcv[1] = l4.y; lcv[2] = l4.z; lcv[3] = l4.w;
+      for (int q = 0; q < SPLIT_PTS; ++q) {
+        const int pt = ps0 + 32 * q;
+        if (pt < A.npt) {
+          const float2 tt = __ldg(A.times_ff + pt);
+          hi[q] = tt.x; lo[q] = tt.y; lcv[q] = __ldg(A.lcids + pt);
         } else {
-#pragma unroll
-          for (int q = 0; q < SPLIT_PTS; ++q) {
-            const int pt = pt0 + q;
-            if (pt < A.npt) {
-              const float2 tt = __ldg(A.times_ff + pt);
-              hi[q] = tt.x; lo[q] = tt.y; lcv[q] = __ldg(A.lcids + pt);
-            } else {
-              hi[q] = 0.0f; lo[q] = 0.0f; lcv[q] = -1;
-            }
-          }
+          hi[q] = 0.0f; lo[q] = 0.0f; lcv[q] = -1;
         }
-        split_tile_points(orb, LCR, ldm_pv, A.ng, A.inv_dg, wide, tm, hi, lo, lcv, L, lane, res);
       }
-      if (full4 && row_vec) {
-        __stcs(reinterpret_cast<float4*>(row + pt0), make_float4(res[0], res[1], res[2], res[3]));
-      } else {
-        for (int q = 0; q < SPLIT_PTS; ++q)
-          if (pt0 + q < A.npt) __stcs(row + pt0 + q, res[q]);
-      }
+      split_tile_points(orb, LCR, ldm_pv, A.ng, A.inv_dg, wide, tm, hi, lo, lcv, L, lane, res);
+#pragma unroll
+      for (int q = 0; q < SPLIT_PTS; ++q)
+        if (ps0 + 32 * q < A.npt) __stcs(row + ps0 + 32 * q, res[q]);
     }
   }
 }
@@ -1290,10 +1313,11 @@ int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, in
   dim3 fg((unsigned)bx, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
   const bool lc_smem = nlc <= LC_SMEM;
   const size_t smem = sizeof(float) * (ORB32 + (lc_smem ? (size_t)nlc * LC32 : 0));
+  cudaStream_t s = as_stream(stream);
   if (lc_smem)
-    flux_split_kernel<true><<<fg, FLUX_NW * 32, smem, as_stream(stream)>>>(fa, (int)chunk);
+    flux_split_kernel<true><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
   else
-    flux_split_kernel<false><<<fg, FLUX_NW * 32, smem, as_stream(stream)>>>(fa, (int)chunk);
+    flux_split_kernel<false><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
   return check_launch("rr_flux_split");
 }
 
