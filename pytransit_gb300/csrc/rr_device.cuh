@@ -79,6 +79,19 @@ __device__ inline R ccia_star(R k, R z, R& kappa0) {
   return R(CUDART_NAN);
 }
 
+// The kite branch of ccia_star<float> (|1 - k| < z <= 1 + k) without
+// branches: the three lengths sorted by a min/max network (exact), then the
+// same expressions in the same order, so the value equals ccia_star<float>'s.
+__device__ __forceinline__ float kite_star_f32(float k, float z) {
+  const float a = fmaxf(1.0f, k), b = fminf(1.0f, k);
+  const float x = fmaxf(a, z), t = fminf(a, z);
+  const float y = fmaxf(b, t), w = fminf(b, t);
+  const float a_kite = 0.5f * sqrtf((x + (y + w)) * (w - (x - y)) * (w + (x - y)) * (x + (y - w)));
+  const float k0 = atan2f(2.0f * a_kite, (k - 1.0f) * (k + 1.0f) + z * z);
+  const float k1 = atan2f(2.0f * a_kite, (1.0f - k) * (1.0f + k) + z * z);
+  return 1.0f * 1.0f * k1 + k * k * k0 - a_kite;
+}
+
 // The same area with its partial derivatives: dA/dk = 2 k kappa0 (the
 // reference's dfdk, common.py:105-114) and dA/dz = -2 A_kite / z (its dfdb,
 // common.py:117-128).

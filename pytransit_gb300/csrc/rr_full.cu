@@ -756,30 +756,37 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
         l0q[q] = need ? __ldg(lda + i) : 0.0f;
         l1q[q] = need ? __ldg(lda + i + 1) : 0.0f;
       }
+      // classification by selects: no overlap (1 - 0 / istar, NaN with a NaN
+      // istar), fully inside (the lerp times pi k^2 / istar) or on the limb
+      const float res_out = 1.0f - 0.0f * invis;
 #pragma unroll
       for (int q = 0; q < SPLIT_PTS; ++q) {
         if (!(act >> q & 1u)) continue;   // warp-uniform
-        if (!(inb >> q & 1u)) {
-          zq[q] = 0.0f;
-        } else if (!(zq[q] < lim_out)) {
-          res[q] = 1.0f - 0.0f * invis;            // no overlap: 1 - 0 / istar (NaN with a NaN istar)
-        } else if (zq[q] <= lim_in) {
-          res[q] = 1.0f - fmaf(frq[q], l1q[q] - l0q[q], l0q[q]) * area_in;
-        } else {
-          limb |= 1u << q;
-        }
+        const bool in = inb >> q & 1u;
+        const bool ovl = zq[q] < lim_out, inner = zq[q] <= lim_in;
+        const float r_in = 1.0f - fmaf(frq[q], l1q[q] - l0q[q], l0q[q]) * area_in;
+        res[q] = in ? (ovl ? (inner ? r_in : res[q]) : res_out) : res[q];
+        limb |= (in && ovl && !inner) ? 1u << q : 0u;
       }
       // Limb points (kite area, two atan2) in place, slot by slot: the limb
       // points of a slot are consecutive in time (an ingress or an egress),
       // so one or two slots of a tile hold them all, and their table values
-      // came with the loads above.
+      // came with the loads above.  For k < 1 every limb point is in the kite
+      // case, evaluated on all lanes of the slot without branches and kept
+      // where the lane's point is on the limb.
 #pragma unroll
       for (int q = 0; q < SPLIT_PTS; ++q) {
         if (!(act >> q & 1u)) continue;                    // warp-uniform
         if (!__ballot_sync(FULL, limb >> q & 1u)) continue;  // warp-uniform
-        if (limb >> q & 1u) {
+        const bool lm = limb >> q & 1u;
+        const float lerp = fmaf(frq[q], l1q[q] - l0q[q], l0q[q]);
+        if (k < 1.0f) {                                    // tile-uniform
+          const float zz = lm ? zq[q] : 1.0f;              // an in-range z for the other lanes
+          const float a = kite_star_f32(k, zz);
+          res[q] = lm ? 1.0f - (lerp * a) * invis : res[q];
+        } else if (lm) {
           float kap;
-          res[q] = 1.0f - (fmaf(frq[q], l1q[q] - l0q[q], l0q[q]) * ccia_star<float>(k, zq[q], kap)) * invis;
+          res[q] = 1.0f - (lerp * ccia_star<float>(k, zq[q], kap)) * invis;
         }
       }
       return;
