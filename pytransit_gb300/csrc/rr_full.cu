@@ -1001,20 +1001,24 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
         cull = !hit;
       }
     }
-    unsigned cmask = __ballot_sync(FULL, cull);
     const int jn = min(32, ntl - j0);
-    int tile = tw0 + j0 * t_step;
-    for (int jt = 0; jt < jn; ++jt, tile += t_step, cmask >>= 1) {
-      if (cmask & 1u) {
-        if (row_vec && tile != tile_part) {
-          __stcs(reinterpret_cast<float4*>(row) + (size_t)tile * (WARP_TILE / 4) + lane, fill4);
-        } else {
-          const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
-          for (int q = 0; q < SPLIT_PTS; ++q)
-            if (pt0 + q < A.npt) __stcs(row + pt0 + q, fill);
-        }
-        continue;
+    const unsigned jmask = jn == 32 ? 0xffffffffu : (1u << jn) - 1u;
+    const unsigned cmask = __ballot_sync(FULL, cull) & jmask;
+    // the culled tiles first, walking the set bits of the mask
+    float4* const row4 = reinterpret_cast<float4*>(row) + lane;
+    for (unsigned m = cmask; m; m &= m - 1u) {
+      const int tile = tw0 + (j0 + __ffs(m) - 1) * t_step;
+      if (row_vec && tile != tile_part) {
+        __stcs(row4 + (size_t)tile * (WARP_TILE / 4), fill4);
+      } else {
+        const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
+        for (int q = 0; q < SPLIT_PTS; ++q)
+          if (pt0 + q < A.npt) __stcs(row + pt0 + q, fill);
       }
+    }
+    // then the tiles that reach a box copy
+    for (unsigned m = ~cmask & jmask; m; m &= m - 1u) {
+      const int tile = tw0 + (j0 + __ffs(m) - 1) * t_step;
       // The tile reaches a box copy (the cull test above said so).  Slot q of
       // lane l holds point tile * 128 + q * 32 + l: each slot is 32
       // consecutive points, coalesced in its loads and stores.
