@@ -588,20 +588,21 @@ __global__ void __launch_bounds__(256) flux_f64_kernel(FluxF64Args A) {
 }
 
 // ---------------------------------------------------------------------------
-// Split-precision flux.  A block owns one pv and loops its 8 warps over warp
-// tiles of 128 consecutive points (4 per lane, float4 loads and stores).  The block
-// first stages the pv's orbit record and its per-light-curve records in
-// shared memory, so the per-point work has no dependent global loads.  A warp
-// tile of one light curve whose time range misses every box copy is written
-// as 1.0 without per-point work.  Otherwise, per point: an FP32 fast test of the phase-folded time against the bounding box
-// widened by the pv's error bound; candidates get the exact phase reduction
-// in FP32 pairs (error-free transformations) and the exact box test; in-box
-// points are compacted into a per-warp list whose (point, sample) pairs are
-// spread over the 32 lanes, each lane evaluating one sample (z, table
-// interpolation, area) in FP32; a segmented shuffle reduction sums the
-// samples of each point.  Output F = 1 - deficit.
+// Split-precision flux.  The output row of a pv is cut into warp tiles of
+// 128 consecutive points.  A block stages the pv's orbit record and its
+// per-light-curve records in shared memory, so the per-point work has no
+// dependent global loads, and its warps take a range of tiles.  A warp tests
+// 32 of its tiles at once against the precomputed tile summaries (one lane
+// per tile): a tile of one light curve whose time range misses every box
+// copy is one 16-byte store of ones per lane.  The other tiles load their
+// FP32-pair times (slot q of lane l holds point q * 32 + l) and take the
+// per-point path: the phase-folded time exact in FP32 pairs (error-free
+// transformations) and the box test; then, in FP32, z, the LD-table lerp and
+// the kite area on the limb, or, with several samples per point, a per-warp
+// list of (point, sample) pairs spread over the lanes and summed with a
+// segmented shuffle reduction.  Output F = 1 - deficit.
 // ---------------------------------------------------------------------------
-constexpr int SPLIT_WARPS = 8;
+constexpr int SPLIT_WARPS = 8;                // warps per block of the serving kernel
 constexpr int SPLIT_PTS = 4;                 // points per lane
 constexpr int WARP_TILE = 32 * SPLIT_PTS;    // points per warp tile
 
@@ -651,14 +652,16 @@ __device__ __forceinline__ float exact_tc(float hi, float lo, float d0h, float d
   return s2 + tail;
 }
 
-// Per-point path for one warp tile of one pv.  Phase-folded times: for a tile
-// of one light curve whose span plus box half-width is below p/2, the exact time of the tile's
-// first point plus each point's (exact, small) offset from it; otherwise a
-// fast FP32 test per point and the exact reduction for candidates.  Then the
-// samples of the in-box points: one lane per point when every in-box point
-// has one sample, else a per-warp list whose (point, sample) pairs are spread
-// over the lanes and summed with a segmented shuffle reduction.  res[] holds
-// 1.0 on entry and the flux of in-box points on exit.
+// Per-point path for one warp tile of one pv (slot q of lane l = the tile's
+// point q * 32 + l).  Phase-folded times: for a tile of one light curve whose
+// span plus box half-width is below p/2, the exact time of the tile's first
+// point plus each point's (exact, small) offset from it; otherwise a fast
+// FP32 test per point and the exact reduction for candidates.  Then the
+// samples of the in-box points: with one sample per point, per point in
+// place, skipping slots without an in-box point as a whole warp; else a
+// per-warp list whose (point, sample) pairs are spread over the lanes and
+// summed with a segmented shuffle reduction.  res[] holds 1.0 on entry and
+// the flux of in-box points on exit.
 __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb, const float* __restrict__ LCR,
                                                   const float* __restrict__ ldm_pv, int ng, float inv_dg,
                                                   bool wide, float4 tm, const float* hi, const float* lo,
@@ -943,11 +946,10 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
 
 // One block's share of one parameter vector: stage the pv's orbit and
 // light-curve records in shared memory, then the warps loop over the tiles
-// t_first + warp, + t_step, ... below t_end.  A tile whose time range (from
-// the precomputed tile summary) misses every box copy of its light curve is
-// written as 1.0 straight away; other tiles load their times and take the
-// per-point path.  Ends without a barrier: the caller synchronises before
-// staging another pv.
+// t_first + warp, + t_step, ... below t_end, 32 at a time: the cull tests,
+// the stores of the culled tiles (walking the set bits of the cull mask),
+// then the per-point path of the others.  Ends without a barrier: the caller
+// synchronises before staging another pv.
 __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, int t_first, int t_step, int t_end,
                                                float* recs, bool lc_in_smem, WarpList* lists) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
