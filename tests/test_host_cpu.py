@@ -58,6 +58,17 @@ def test_argument_errors_without_gpu():
                        None, None, None, None, None, 256, 100, 40, 0.1, 0.005, 0.5, 0.01, None, None, 16,
                        None, 10, None)
     assert st == 3
+    # the fused split prologue: device pointers are only passed on, never read on the host
+    dev = ctypes.c_void_p(256)
+
+    def prepare_ld(law, nkc, npb, wsb):
+        return L.rr_prepare_split_ld(0.0, 1.0, dev, nkc, dev, 1, 1, dev, dev, dev, dev, dev, 8, 1, npb, dev, dev,
+                                     dev, dev, law, dev, 2, dev, 40, dev, 3, dev, 256, 100, 0.002, 0.005, 0.5,
+                                     dev, dev, dev, dev, wsb, None)
+    big = L.rr_full_split_workspace_bytes(8, 4, 1, 1, 100)
+    assert prepare_ld(2, 3, 4, big) == 1          # k with 3 columns and 4 passbands
+    assert prepare_ld(2, 1, 4, 64) == 3           # workspace too small
+    assert prepare_ld(99, 1, 4, big) == 5         # unknown law: the two-stage path's check
 
 
 def test_z_grid_matches_oracle():
