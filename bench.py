@@ -16,7 +16,8 @@ Reported (one JSON line from rank 0):
   roofline   the flux kernel's algorithmic bytes / its event-timed duration
              against the measured HBM copy bandwidth;
   cpu_baseline  the oracle's FP64 C port (OpenMP, all host cores) on a
-             bounded sample of the same workload.
+             bounded sample of the same workload, and at 1 thread (the
+             reference's default nthreads=1) on a smaller sample.
 ``--impl reference`` times that CPU implementation alone (the reference's
 path restated in C; the reference itself is Python + numba, absent here).
 """
@@ -169,9 +170,19 @@ def run_cpu_baseline(data, prm, budget_s=12.0, npv_sample=8192):
         reps += 1
     npt = data["time"].size
     value = reps * npv_sample * npt / t_total
+    # the reference's default is one thread (nthreads=1): a bounded sample at 1 thread beside it
+    npv_1, reps_1, t_1 = 256, 0, 0.0
+    while t_1 < 3.0 and reps_1 < 100:
+        t = time.perf_counter()
+        cpu_rr_full(m, prm, npv_1, 1)
+        t_1 += time.perf_counter() - t
+        reps_1 += 1
+    value_1 = reps_1 * npv_1 * npt / t_1
     return {"value": value, "unit": "model points/s", "cores": ncores, "kind": "port",
             "sample": f"{npv_sample} of 8192 parameter vectors x {npt} times, {reps} repetitions, "
-                      f"{t_total:.1f} s (oracle/rr_oracle.c rr_full restatement, OpenMP, FP64)"}
+                      f"{t_total:.1f} s (oracle/rr_oracle.c rr_full restatement, OpenMP, FP64)",
+            "value_1_thread": value_1,
+            "sample_1_thread": f"{npv_1} parameter vectors x {npt} times, {reps_1} repetitions, {t_1:.1f} s"}
 
 
 def impl_reference(args, rank):
