@@ -274,6 +274,37 @@ def bench_c2(torch, device, steps=5):
             "timed": "RoadRunnerModel.evaluate(copy=False), CUDA events, parameters uploaded each call"}
 
 
+def bench_ts(torch, device, steps=5, npv=64, npb=200, npt=19700):
+    """Transmission spectroscopy: 64 pv x 200 channels x 19,700 times (2-min
+    cadence), quadratic LD, k ~ U(0.09, 0.11), one sample per point."""
+    from pytransit_gb300 import TSModel
+    rng = np.random.default_rng(4242)
+    T = 2459000.0
+    time_ = T + np.arange(npt) * (2.0 / 1440.0)
+    a = rng.uniform(3.0, 20.0, npv)
+    prm = dict(k=rng.uniform(0.09, 0.11, (npv, npb)),
+               ldc=np.stack([rng.uniform(0, .6, (npv, npb)), rng.uniform(0, .3, (npv, npb))], -1),
+               t0=T + 13.7 + rng.normal(0, 1e-3, npv), p=rng.uniform(0.5, 15.0, npv), a=a,
+               i=np.arccos(rng.uniform(0.0, 0.9, npv) / a), e=np.zeros(npv), w=np.zeros(npv))
+    res = {}
+    for prec in ("split", "fp64"):
+        m = TSModel('quadratic', precision=prec, device=device)
+        m.set_data(time_)
+        res[prec] = bench_model(m, prm, steps if prec == "split" else 2, torch, device)
+    dF = float((res["split"][1].double() - res["fp64"][1]).abs().max().item())
+    pts = npv * npb * npt
+    out_bytes = pts * 4
+    peak, _ = measured_peaks()
+    return {"workload": f"TSModel, {npv} pv x {npb} channels x {npt} times (2-min cadence), quadratic LD, nsamples=1",
+            "split_points_per_s": pts / (res["split"][0] / 1e3), "fp64_points_per_s": pts / (res["fp64"][0] / 1e3),
+            "split_ms": res["split"][0], "fp64_ms": res["fp64"][0],
+            "split_over_fp64": res["fp64"][0] / res["split"][0], "max_abs_dF_vs_fp64": dF,
+            "split_output_gbs": out_bytes / (res["split"][0] / 1e3) / 1e9,
+            "split_output_frac_of_hbm": out_bytes / (res["split"][0] / 1e3) / 1e9 / peak,
+            "timed": "TSModel.evaluate(copy=False) (prologue, 2D LD tables and flux), CUDA events, "
+                     "parameters uploaded each call"}
+
+
 def bench_c3(torch, device, steps=3):
     """Log-likelihood + adjoint gradient, 4096 pv x 5000 times, 5 supersamples."""
     from pytransit_gb300 import RoadRunnerModel
@@ -478,8 +509,9 @@ def main():
     ap.add_argument("--npt", type=int, default=19700)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the precision and gradient workloads")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "serve"],
-                    help="c1: the default line; c2 / c3: the precision / gradient workload alone; serve: Poisson stream")
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "ts", "serve"],
+                    help="c1: the default line; c2 / c3 / ts: the precision / gradient / transmission-spectroscopy "
+                         "workload alone; serve: Poisson stream")
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--nreq", type=int, default=300)
     ap.add_argument("--plain-sample", type=int, default=100000)
@@ -494,12 +526,12 @@ def main():
         return impl_reference(args, rank)
     if args.workload == "serve":
         return bench_serve(args) if rank == 0 else 0
-    if args.workload in ("c2", "c3"):
+    if args.workload in ("c2", "c3", "ts"):
         if rank == 0:
             import torch
             device = torch.device("cuda", 0)
             torch.cuda.set_device(device)
-            fn = bench_c2 if args.workload == "c2" else bench_c3
+            fn = {"c2": bench_c2, "c3": bench_c3, "ts": bench_ts}[args.workload]
             print(json.dumps({"workload": args.workload, **fn(torch, device)}), flush=True)
         return 0
 
@@ -681,6 +713,7 @@ def main():
     if rank == 0 and not args.no_extra:
         line["c2_precision"] = bench_c2(torch, device)
         line["c3_gradient"] = bench_c3(torch, device)
+        line["ts"] = bench_ts(torch, device)
         line["eclipse"] = bench_eclipse(torch, device, data, prm)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_baseline(data, prm)
