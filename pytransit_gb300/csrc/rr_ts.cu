@@ -219,8 +219,9 @@ __device__ __forceinline__ bool ts_sample(R t, const R* cc, R kmean, R inv1pk, R
 constexpr int TS_MW = 8;      // LD-table rows a lane keeps weights for
 constexpr int TS_SCOLS = 16;  // LD-table columns a warp stages per round
 
-// One warp tile (128 points, 4 per lane) of one pv at a time.  The tile's
-// channel rows are first filled with 1.0 (float4 stores).  In-box points are
+// A block owns a contiguous range of warp tiles (128 points, 4 per lane) of
+// one pv.  The range's channel rows are first filled with 1.0, row by row;
+// then each warp takes a tile at a time.  In-box points are
 // then taken 32 at a time, one per lane, consecutive points in consecutive
 // lanes: a lane folds its exposure samples into weights on at most TS_MW
 // consecutive rows of the LD-mean tables, since for every channel b
@@ -260,23 +261,37 @@ ts_flux_kernel(const double* __restrict__ times, const float2* __restrict__ time
   const double tz = SPLIT ? 0.0 : t0[pv], pp = SPLIT ? 0.0 : p[pv];
   const bool vec_ok = ((ldflux & 3) == 0) && ((reinterpret_cast<uintptr_t>(flux) & 15) == 0) && sizeof(R) == 4;
 
-  for (int tile = blockIdx.x * TS_WARPS + warp; tile < ntiles; tile += gridDim.x * TS_WARPS) {
-    const int pt0 = tile * 128 + lane * 4;
-    const bool full4 = pt0 + 4 <= npt;
-    // ones (or NaN) for every channel
+  // The block owns the contiguous tiles [tb0, tb1).  First its warps fill
+  // every channel row of that range with ones (NaN for an invalid pv), row by
+  // row: each row segment is one contiguous run, so the output stream reaches
+  // DRAM in long runs rather than 512-byte pieces scattered over npb rows.
+  // After the block barrier, warps take the tiles and overwrite the in-box
+  // points.
+  const int tpb = (ntiles + gridDim.x - 1) / gridDim.x;
+  const int tb0 = blockIdx.x * tpb, tb1 = min(ntiles, tb0 + tpb);
+  if (tb0 >= tb1) return;   // block-uniform
+  {
     const R fill = valid ? R(1) : R(CUDART_NAN);
-    for (int b = 0; b < npb; ++b) {
+    const int p0 = tb0 * 128, p1 = min(npt, tb1 * 128);
+    for (int b = warp; b < npb; b += TS_WARPS) {
       R* row = fpv + (size_t)b * ldflux;
+      int pt = p0 + lane;
       if constexpr (sizeof(R) == 4) {
-        if (full4 && vec_ok) {
-          __stcs(reinterpret_cast<float4*>(row + pt0), make_float4(fill, fill, fill, fill));
-          continue;
+        if (vec_ok) {
+          const int n4 = (p1 - p0) >> 2;   // whole float4s from p0 (a multiple of 4)
+          float4* r4 = reinterpret_cast<float4*>(row + p0);
+          for (int i = lane; i < n4; i += 32) __stcs(r4 + i, make_float4(fill, fill, fill, fill));
+          pt = p0 + 4 * n4 + lane;
         }
       }
-      for (int q = 0; q < 4; ++q)
-        if (pt0 + q < npt) row[pt0 + q] = fill;
+      for (; pt < p1; pt += 32) row[pt] = fill;
     }
-    if (!valid) continue;
+  }
+  __syncthreads();
+  if (!valid) return;       // block-uniform
+
+  for (int tile = tb0 + warp; tile < tb1; tile += TS_WARPS) {
+    const int pt0 = tile * 128 + lane * 4;
     // tile cull (split: from the tile summary)
     if (SPLIT && !(o[22] != R(0))) {
       const float4 tm = __ldg(meta + tile);
@@ -302,7 +317,6 @@ ts_flux_kernel(const double* __restrict__ times, const float2* __restrict__ time
     const unsigned bq0 = __ballot_sync(FULL, inb & 1u), bq1 = __ballot_sync(FULL, inb >> 1 & 1u);
     const unsigned bq2 = __ballot_sync(FULL, inb >> 2 & 1u), bq3 = __ballot_sync(FULL, inb >> 3 & 1u);
     if ((bq0 | bq1 | bq2 | bq3) == 0u) continue;
-    __syncwarp();   // the ones above are visible before the in-box values overwrite them
 
     for (int r = 0; r < 4; ++r) {
       // lane <-> tile point r*32 + lane, owned in the fill above by lane (r*32+lane)/4
