@@ -158,3 +158,18 @@ def test_serving_struct_layout_matches_binding():
                    ('flux', 'u8'), ('ldflux', 'i8'), ('npt', 'i4'), ('npv', 'i4'), ('nlc', 'i4'), ('npb', 'i4'),
                    ('ng', 'i4'), ('pad0', 'i4'), ('inv_dg', 'f4'), ('pad1', 'f4')])
     assert rs.value == dt.itemsize and its.value == 24
+
+
+def test_bench_reads_the_profiled_traffic_and_peak():
+    """bench.py's roofline.traffic comes from the committed ncu summary of the
+    flux kernel (bytes per point x the launch's points); the summary must keep
+    the line it parses, with a value near the algorithmic 4 B per point."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    t = bench.profiled_traffic(8192, 19700)
+    assert t is not None
+    bpp = t / (8192 * 19700)
+    assert 3.0 < bpp < 4.5, bpp
+    peak, kind = bench.measured_peaks()
+    assert peak > 1000 and kind in ("measured", "fallback")
