@@ -71,7 +71,8 @@ def measured_peaks():
 
 def profiled_traffic(npv, npt):
     """DRAM bytes per launch of the split flux kernel from the committed ncu
-    summary (profiles/flux_split_c1.md), scaled to this launch's points."""
+    summary of that kernel (its traffic_bytes_per_point line), scaled to this
+    launch's points."""
     path = os.path.join(ROOT, "profiles", "flux_split_c1.md")
     if not os.path.exists(path):
         return None
