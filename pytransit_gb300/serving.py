@@ -18,7 +18,11 @@ scheduler thread owns the GPU:
   graph; requests admitted while a step runs join the next one, so work from
   many requests overlaps on the device;
 * completion: a request whose last items ran is copied to pinned host memory
-  on a copy stream and its future resolved; latency = resolve - submit.
+  on a copy stream and its future resolved; latency = resolve - submit;
+* failures: an exception in a request's set-up, in a step or in a copy fails
+  the futures of the requests concerned (``stats.failed``; memory refusals
+  count as ``stats.rejected``) and the loop goes on serving the others; a
+  future cancelled while queued is dropped at admission.
 
 The GPU work is behind ``GpuExecutor`` so that the scheduling logic can be
 exercised on the CPU with a fake executor (tests/test_serving_cpu.py).
@@ -38,7 +42,7 @@ import numpy as np
 
 from . import ldmodels as _ldm
 
-__all__ = ['Request', 'RRServer', 'GpuExecutor', 'ServerStats']
+__all__ = ['Request', 'RRServer', 'GpuExecutor', 'ServerStats', 'ServedFuture']
 
 TILE = 128
 
@@ -71,21 +75,42 @@ class Request:
 
 @dataclass
 class ServerStats:
+    """Counters of a server.  ``rejected``: requests refused for memory (larger
+    than the budget or the arena); ``failed``: requests whose set-up, launch or
+    copy raised; ``cancelled``: futures the caller cancelled while queued;
+    ``bypassed``: admissions that passed a blocked request at the head of the
+    queue."""
     submitted: int = 0
     admitted: int = 0
     completed: int = 0
     rejected: int = 0
+    failed: int = 0
+    cancelled: int = 0
+    bypassed: int = 0
     steps: int = 0
     points: int = 0
     peak_bytes: int = 0
+    max_queue: int = 0
     latencies: list = field(default_factory=list)
+    done_times: list = field(default_factory=list)
 
     def summary(self):
         lat = np.array(self.latencies) if self.latencies else np.zeros(1)
         return dict(submitted=self.submitted, admitted=self.admitted, completed=self.completed,
-                    rejected=self.rejected, steps=self.steps, points=self.points,
-                    peak_hbm_bytes=self.peak_bytes, p50_s=float(np.percentile(lat, 50)),
+                    rejected=self.rejected, failed=self.failed, cancelled=self.cancelled, bypassed=self.bypassed,
+                    steps=self.steps, points=self.points, peak_hbm_bytes=self.peak_bytes,
+                    max_queue=self.max_queue, p50_s=float(np.percentile(lat, 50)),
                     p99_s=float(np.percentile(lat, 99)), mean_s=float(lat.mean()))
+
+
+class ServedFuture(cf.Future):
+    """The future of one request.  Besides the result it carries
+    ``error_bound``: the request's maximum absolute flux error against the
+    FP64 model, set before the result (None where the executor states none)."""
+
+    def __init__(self):
+        super().__init__()
+        self.error_bound = None
 
 
 def shape_request(req: Request):
@@ -233,12 +258,23 @@ class RRServer:
     """Continuous-batching server (see the module docstring)."""
 
     def __init__(self, executor=None, hbm_budget: float = 120e9, step_items: int = 4096,
-                 ts_chunk_bytes: float = 4e9, device=None, result: str = 'host', freeze_gc: bool = True):
+                 ts_chunk_bytes: float = 4e9, device=None, result: str = 'host', freeze_gc: bool = True,
+                 hol_max_wait_s: float = 0.1, admit_scan: int = 64):
         """freeze_gc: move every object that exists when the server starts (the
         imported modules of torch, numpy, ...) out of the cyclic garbage
         collector's generations (gc.freeze), so that a full collection during
         serving scans only the objects made since, not pausing every thread
-        for tens of milliseconds."""
+        for tens of milliseconds.
+
+        Admission is in arrival order, except that a request at the head of the
+        queue that does not fit yet lets later requests that fit pass it (up to
+        ``admit_scan`` requests deep) until it has waited ``hol_max_wait_s``;
+        from then on nothing passes it, so the memory that running requests
+        give back goes to it."""
+        step_items = int(step_items)
+        max_items = getattr(executor, 'MAX_ITEMS', GpuExecutor.MAX_ITEMS)
+        if not 1 <= step_items <= max_items:
+            raise ValueError(f"step_items must be in [1, {max_items}], got {step_items}")
         self.ex = executor if executor is not None else GpuExecutor(
             device, result=result, arena_bytes=int(hbm_budget * 1.1) + (1 << 30))
         if freeze_gc:
@@ -247,6 +283,8 @@ class RRServer:
         self.budget = int(hbm_budget)
         self.step_items = step_items
         self.ts_chunk_bytes = ts_chunk_bytes
+        self.hol_max_wait_s = float(hol_max_wait_s)
+        self.admit_scan = max(1, int(admit_scan))
         self.stats = ServerStats()
         self._ids = itertools.count()
         self._queue = collections.deque()
@@ -272,12 +310,14 @@ class RRServer:
             raise ValueError(f"unknown limb darkening law {ld}")
         req = Request(kind=kind, ld=ld, data=data, params=params)
         req.state['keep'] = keep_result
-        req.future = cf.Future()
+        req.future = ServedFuture()
         req.rid = next(self._ids)
         req.t_submit = time.perf_counter()
         shape_request(req)
         req.nbytes = request_bytes(req)
         with self._cv:
+            if self._stop:
+                raise RuntimeError("the server is closed")
             self.stats.submitted += 1
             if self._min_bytes(req) > self.budget:
                 self.stats.rejected += 1
@@ -286,6 +326,7 @@ class RRServer:
                     f"more than the {self.budget / 1e9:.1f} GB budget"))
                 return req.future
             self._queue.append(req)
+            self.stats.max_queue = max(self.stats.max_queue, len(self._queue))
             self._cv.notify()
         return req.future
 
@@ -301,11 +342,18 @@ class RRServer:
         t0 = time.perf_counter()
         while True:
             with self._cv:
-                if not self._queue and not self._active:
+                if not self._queue and not self._active and not self._issued:
                     return True
             if timeout is not None and time.perf_counter() - t0 > timeout:
                 return False
             time.sleep(0.001)
+
+    def load(self):
+        """The server's load now: queued requests, admitted requests and the
+        device bytes they hold against the budget."""
+        with self._cv:
+            return dict(queued=len(self._queue), active=len(self._active), admitted_bytes=self._used,
+                        budget_bytes=self.budget)
 
     # -- scheduler ----------------------------------------------------------
     def _min_bytes(self, req):
@@ -315,32 +363,53 @@ class RRServer:
         return req.nbytes
 
     def _admit(self):
-        """Admit queued requests in order while the budget allows; a request
-        the executor cannot place yet (device memory fragmented) waits at
-        the head of the queue for the next completion."""
+        """Admit queued requests while the budget allows, in arrival order.  A
+        request that does not fit yet (budget, or device memory fragmented)
+        keeps its place; later requests that fit may pass it until the
+        request at the head has waited hol_max_wait_s.  A request whose
+        future the caller cancelled is dropped here."""
+        pos = 0                        # queue position of the next candidate
         while True:
             with self._cv:
-                if not self._queue:
+                if pos >= len(self._queue) or pos >= self.admit_scan:
                     return
-                req = self._queue[0]
+                head = self._queue[0]
+                if pos > 0 and time.perf_counter() - head.t_submit > self.hol_max_wait_s:
+                    return             # the head has waited long enough: memory is kept for it
+                req = self._queue[pos]
+                if req.future.cancelled():
+                    del self._queue[pos]
+                    self.stats.cancelled += 1
+                    continue
                 need = self._min_bytes(req)
                 if self._used + need > self.budget:
-                    return
-                self._queue.popleft()
+                    pos += 1
+                    continue
+                if not req.state.get('running'):
+                    # from here on the caller can no longer cancel it
+                    if not req.future.set_running_or_notify_cancel():
+                        del self._queue[pos]
+                        self.stats.cancelled += 1
+                        continue
+                    req.state['running'] = True
+                del self._queue[pos]
                 self._used += need
                 req.state['held'] = need
                 self.stats.peak_bytes = max(self.stats.peak_bytes, self._used)
+                if pos > 0:
+                    self.stats.bypassed += 1
             req.t_admit = time.perf_counter()
             try:
                 placed = self.ex.setup(req, self.ts_chunk_bytes)
-            except Exception as exc:   # pragma: no cover - surfaced to the client
+            except Exception as exc:
                 self._finish(req, exc)
                 continue
             if placed is False:
                 with self._cv:
                     self._used -= req.state.pop('held')
-                    self._queue.appendleft(req)
-                return
+                    self._queue.insert(pos, req)
+                pos += 1
+                continue
             if req.kind == 'rr':
                 req.state['items'] = work_items(req.npv, req.npt)
                 req.state['icur'] = 0
@@ -372,26 +441,44 @@ class RRServer:
         return batch
 
     def _finish(self, req, result):
+        """Resolve a request's future and give its memory back.  Called once
+        per admitted request; an exception as the result fails it."""
         req.t_done = time.perf_counter()
+        failed = isinstance(result, BaseException)
         with self._cv:
             self._active.pop(req.rid, None)
-            self._used -= req.state.get('held', 0)
-            if isinstance(result, Exception):
-                self.stats.rejected += 1
+            self._issued.pop(req.rid, None)
+            self._used -= req.state.pop('held', 0)
+            if failed:
+                if isinstance(result, MemoryError):
+                    self.stats.rejected += 1
+                else:
+                    self.stats.failed += 1
             else:
                 self.stats.completed += 1
                 self.stats.points += req.points
                 self.stats.latencies.append(req.t_done - req.t_submit)
-        self.ex.release(req)
-        if isinstance(result, Exception):
+                self.stats.done_times.append(req.t_done)
+        try:
+            self.ex.release(req)
+        except Exception as exc:       # the request's result stands; the executor's error is kept
+            self._release_errors.append(exc)
+        if failed:
             req.future.set_exception(result)
         else:
             if not req.state.get('keep', True):
                 req.state.pop('host_out', None)
                 result = req.points
+            req.future.error_bound = req.state.get('error_bound')
             req.future.set_result(result)
 
+    def _fail_all(self, reqs, exc):
+        for r in {id(r): r for r in reqs}.values():
+            if r.rid in self._active or r.rid in self._issued:
+                self._finish(r, exc)
+
     def _loop(self):
+        self._release_errors = []
         while True:
             with self._cv:
                 if self._stop and not self._queue and not self._active:
@@ -399,31 +486,47 @@ class RRServer:
                 if not self._queue and not self._active:
                     self._cv.wait(timeout=0.01)
                     continue
-            self._admit()
-            batch = self._take_items()
-            ts_work, self._ts_new = self._ts_new, []
-            if batch or ts_work:
-                self.ex.step(batch, ts_work)
-                self.stats.steps += 1
-                for r in ts_work:
-                    self._issued[r.rid] = r
-                for r in {id(r): r for r, _ in batch}.values():
-                    if r.state['icur'] >= len(r.state['items']):
+            try:
+                self._admit()
+                batch = self._take_items()
+                ts_work, self._ts_new = self._ts_new, []
+                if batch or ts_work:
+                    try:
+                        self.ex.step(batch, ts_work)
+                    except Exception as exc:
+                        # the step's requests fail; requests not in it keep going
+                        self._fail_all([r for r, _ in batch] + ts_work, exc)
+                        batch, ts_work = [], []
+                    self.stats.steps += 1
+                    for r in ts_work:
                         self._issued[r.rid] = r
-            # completions, polled in issue order: stop at the few oldest still running
-            pending = 0
-            for r in list(self._issued.values()):
-                if not r.state.get('copy_started'):
-                    self.ex.start_copy(r)
-                    r.state['copy_started'] = True
-                done = self.ex.poll_copy(r)
-                if done is not None:
-                    del self._issued[r.rid]
-                    self._finish(r, done)
-                else:
-                    pending += 1
-                    if pending >= 4:
-                        break
+                    for r in {id(r): r for r, _ in batch}.values():
+                        if r.state['icur'] >= len(r.state['items']):
+                            self._issued[r.rid] = r
+                # completions, polled in issue order: stop at the few oldest still running
+                pending = 0
+                for r in list(self._issued.values()):
+                    try:
+                        if not r.state.get('copy_started'):
+                            self.ex.start_copy(r)
+                            r.state['copy_started'] = True
+                        done = self.ex.poll_copy(r)
+                    except Exception as exc:
+                        self._finish(r, exc)
+                        continue
+                    if done is not None:
+                        self._finish(r, done)
+                    else:
+                        pending += 1
+                        if pending >= 4:
+                            break
+            except Exception as exc:
+                # a fault of the scheduler itself: every request it holds fails
+                # rather than waiting forever; queued requests are served after
+                self._fail_all(list(self._active.values()) + list(self._issued.values()), RuntimeError(
+                    f"serving loop error: {exc!r}"))
+                self._ts_new = []
+                batch, ts_work = [], []
             if not batch and not ts_work:
                 time.sleep(0.0002)
         self.ex.shutdown()
@@ -650,6 +753,9 @@ class GpuExecutor:
                 n = sum(len(w) for _, w in batch)
                 nb = 4 * (n * 6 + 1)
                 lo = self.ring.alloc(nb)
+                if lo is None:
+                    raise RuntimeError(f"a step's item list ({nb} bytes) does not fit the {self.ring.size}-byte "
+                                       "pinned staging ring")
                 buf = self.ring.np[lo:lo + nb].view(np.int32)
                 rows = buf[:n * 6].reshape(n, 6)
                 c = 0
@@ -757,11 +863,17 @@ class GpuExecutor:
         ev = req.state.get('copy_event')
         if ev is None or not ev.query():
             return None
+        req.state['copy_done'] = True
         out = req.state['host_out']
         return out if self.result == 'device' else out.numpy()
 
     def release(self, req):
-        """Called once the request's GPU work and copies have completed."""
+        """Give a finished request's slot and device memory back.  A request
+        that failed may still have work in flight on the GPU: the device is
+        synchronised first, so that no later request is handed memory that a
+        running kernel or copy still writes."""
+        if not req.state.get('copy_done') and 'g' in req.state:
+            self.torch.cuda.synchronize(self.device)
         slot = req.state.pop('slot', None)
         if slot is not None:
             self.free_slots.append(slot)

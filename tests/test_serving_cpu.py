@@ -32,7 +32,7 @@ class FakeExecutor:
 
     def poll_copy(self, req):
         shape = (req.npv, req.npb_out, req.npt) if req.kind == 'ts' else (req.npv, req.npt)
-        return np.full(shape, float(req.rid))
+        return np.broadcast_to(np.float64(req.rid), shape)    # a view: no memory for large shapes
 
     def release(self, req):
         self.log.append(('release', req.rid))
@@ -123,3 +123,165 @@ def test_unknown_law_and_kind():
     with pytest.raises(ValueError):
         srv.submit('xx', 'quadratic', *rr_req(1, 10))
     srv.close()
+
+
+class FailingExecutor(FakeExecutor):
+    """Raises in set-up, step or poll for the requests whose npv is in the
+    matching set; everything else completes normally."""
+
+    def __init__(self, fail_setup=(), fail_step=(), fail_poll=()):
+        super().__init__()
+        self.fail_setup, self.fail_step, self.fail_poll = set(fail_setup), set(fail_step), set(fail_poll)
+        self.released = []
+
+    def setup(self, req, ts_chunk_bytes):
+        if req.npv in self.fail_setup:
+            raise RuntimeError(f"set-up of {req.rid} failed")
+        super().setup(req, ts_chunk_bytes)
+
+    def step(self, batch, ts):
+        if any(r.npv in self.fail_step for r, _ in batch) or any(r.npv in self.fail_step for r in ts):
+            raise RuntimeError("launch failed")
+        super().step(batch, ts)
+
+    def poll_copy(self, req):
+        if req.npv in self.fail_poll:
+            raise RuntimeError(f"copy of {req.rid} failed")
+        return super().poll_copy(req)
+
+    def release(self, req):
+        self.released.append(req.rid)
+        super().release(req)
+
+
+@pytest.mark.parametrize("where", ["setup", "poll"])
+def test_executor_failure_fails_only_its_request(where):
+    ex = FailingExecutor(**{f"fail_{where}": {7}})
+    srv = RRServer(executor=ex, hbm_budget=1e12, step_items=4)
+    good = [srv.submit('rr', 'quadratic', *rr_req(5, 1000)) for _ in range(3)]
+    bad = srv.submit('rr', 'quadratic', *rr_req(7, 1000))
+    later = srv.submit('rr', 'quadratic', *rr_req(5, 1000))
+    with pytest.raises(RuntimeError):
+        bad.result(timeout=10)
+    for f in good + [later]:
+        assert f.result(timeout=10).shape == (5, 1000)
+    srv.close()
+    st = srv.stats.summary()
+    assert st['failed'] >= 1 and st['rejected'] == 0
+    assert st['completed'] + st['failed'] == 5
+    assert srv._used == 0                         # every admitted byte was given back
+    if where == "poll":
+        assert 3 in ex.released                   # the failed request (the fourth, rid 3) was released
+
+
+def test_step_failure_fails_the_whole_step_and_the_loop_goes_on():
+    """A launch that raises fails every request with items in that step (their
+    device state is unknown); requests admitted later are served."""
+    gate = threading.Event()
+
+    class Held(FailingExecutor):
+        def setup(self, req, ts_chunk_bytes):
+            gate.wait(10)                          # both requests queue up, then join one step
+            super().setup(req, ts_chunk_bytes)
+
+    ex = Held(fail_step={9})
+    srv = RRServer(executor=ex, hbm_budget=1e12, step_items=64)
+    fs = [srv.submit('rr', 'quadratic', *rr_req(9, 500)), srv.submit('rr', 'quadratic', *rr_req(4, 500))]
+    gate.set()
+    for f in fs:
+        with pytest.raises(RuntimeError):
+            f.result(timeout=10)
+    ok = srv.submit('rr', 'quadratic', *rr_req(3, 500))
+    assert ok.result(timeout=10).shape == (3, 500)
+    srv.close()
+    assert srv.stats.failed == 2 and srv.stats.completed == 1
+    assert sorted(ex.released) == [0, 1, 2]
+    assert srv._used == 0
+
+
+def test_cancelled_while_queued_is_dropped():
+    gate = threading.Event()
+
+    class Slow(FakeExecutor):
+        def setup(self, req, ts_chunk_bytes):
+            gate.wait(10)
+            super().setup(req, ts_chunk_bytes)
+
+    ex = Slow()
+    srv = RRServer(executor=ex, hbm_budget=1e12)
+    first = srv.submit('rr', 'quadratic', *rr_req(2, 300))
+    time.sleep(0.05)                               # the loop is inside first's set-up
+    second = srv.submit('rr', 'quadratic', *rr_req(2, 300))
+    assert second.cancel()
+    gate.set()
+    assert first.result(timeout=10).shape == (2, 300)
+    assert second.cancelled()
+    srv.close()
+    st = srv.stats.summary()
+    assert st['cancelled'] == 1 and st['completed'] == 1 and st['failed'] == 0
+    assert ('setup', 1) not in ex.log
+    # a running request can no longer be cancelled
+    assert not first.cancel()
+
+
+def test_small_requests_pass_a_blocked_head_until_it_has_waited():
+    """A big request that does not fit yet must not hold back small ones that
+    do; once it has waited hol_max_wait_s nothing passes it any more."""
+    gate = threading.Event()
+
+    class Gate(FakeExecutor):
+        def poll_copy(self, req):
+            if req.npv == 50 and not gate.is_set():
+                return None                        # the first big request runs until the gate opens
+            return super().poll_copy(req)
+
+    big = Request('rr', 'quadratic', *rr_req(50, 20000))
+    shape_request(big)
+    budget = int(request_bytes(big) * 1.5)         # one big request at a time
+    ex = Gate()
+    srv = RRServer(executor=ex, hbm_budget=budget, hol_max_wait_s=0.3)
+    f_big1 = srv.submit('rr', 'quadratic', *rr_req(50, 20000))
+    time.sleep(0.05)
+    f_big2 = srv.submit('rr', 'quadratic', *rr_req(50, 20000))     # blocked behind big1
+    small = [srv.submit('rr', 'quadratic', *rr_req(1, 500)) for _ in range(3)]
+    for f in small:
+        assert f.result(timeout=5).shape == (1, 500)               # passed the blocked head
+    assert not f_big2.done()
+    assert srv.stats.bypassed >= 3
+    time.sleep(0.35)                               # big2 has now waited longer than hol_max_wait_s
+    late = srv.submit('rr', 'quadratic', *rr_req(1, 500))
+    time.sleep(0.1)
+    assert not late.done()                         # memory is kept for the head
+    gate.set()
+    assert f_big1.result(timeout=5).shape == (50, 20000)
+    assert f_big2.result(timeout=5).shape == (50, 20000)
+    assert late.result(timeout=5).shape == (1, 500)
+    srv.close()
+    assert srv.stats.peak_bytes <= budget
+
+
+def test_step_items_is_checked_at_construction():
+    with pytest.raises(ValueError):
+        RRServer(executor=FakeExecutor(), step_items=10 ** 6)
+    with pytest.raises(ValueError):
+        RRServer(executor=FakeExecutor(), step_items=0)
+
+
+def test_submit_after_close_raises():
+    srv = RRServer(executor=FakeExecutor())
+    srv.close()
+    with pytest.raises(RuntimeError):
+        srv.submit('rr', 'quadratic', *rr_req(1, 10))
+
+
+def test_served_future_carries_the_error_bound():
+    class Bounded(FakeExecutor):
+        def poll_copy(self, req):
+            req.state['error_bound'] = 1e-7 * req.npv
+            return super().poll_copy(req)
+
+    srv = RRServer(executor=Bounded())
+    f = srv.submit('rr', 'quadratic', *rr_req(3, 100))
+    f.result(timeout=5)
+    srv.close()
+    assert f.error_bound == pytest.approx(3e-7)
