@@ -17,7 +17,13 @@ Reported (one JSON line from rank 0):
              against the measured HBM copy bandwidth;
   cpu_baseline  the oracle's FP64 C port (OpenMP, all host cores) on a
              bounded sample of the same workload, and at 1 thread (the
-             reference's default nthreads=1) on a smaller sample.
+             reference's default nthreads=1) on a smaller sample;
+  parity_vs_oracle  the GPU's FP64 and split results for the whole workload
+             against the oracle's FP64 flux of the same workload;
+  serve      the serving leg: a Poisson stream of the mixed-request workload
+             through RRServer (p50/p99 latency, offered vs achieved rate, the
+             highest sustained rate, vs the plain FP64 path per request);
+  c2_precision / c3_gradient / ts / eclipse  the other workloads.
 ``--impl reference`` times that CPU implementation alone (the reference's
 path restated in C; the reference itself is Python + numba, absent here).
 """
@@ -157,17 +163,22 @@ def cpu_oracle_model(data):
     return m
 
 
-def run_cpu_baseline(data, prm, budget_s=12.0, npv_sample=8192):
+def run_cpu_baseline(data, prm, budget_s=12.0, npv_sample=8192, keep=None):
     """The oracle's C port of rr_full on all host cores, on the first
-    npv_sample parameter vectors of the workload, repeated for ~budget_s."""
+    npv_sample parameter vectors of the workload, repeated for ~budget_s.
+    keep: a dict that receives the flux of the first repetition (the FP64
+    result the GPU paths are checked against)."""
     ncores = os.cpu_count() or 1
     m = cpu_oracle_model(data)
     cpu_rr_full(m, prm, 16, ncores)          # warm-up (thread pool, pages)
     reps, t_total = 0, 0.0
     while t_total < budget_s and reps < 1000:
         t = time.perf_counter()
-        cpu_rr_full(m, prm, npv_sample, ncores)
+        f = cpu_rr_full(m, prm, npv_sample, ncores)
         t_total += time.perf_counter() - t
+        if reps == 0 and keep is not None:
+            keep["flux"] = f
+        del f
         reps += 1
     npt = data["time"].size
     value = reps * npv_sample * npt / t_total
@@ -192,7 +203,7 @@ def impl_reference(args, rank):
     data, prm = workload()
     ncores = os.cpu_count() or 1
     m = cpu_oracle_model(data)
-    npv_sample = 2048
+    npv_sample = prm["p"].size             # the whole population: the same workload as the GPU arm
     npt = data["time"].size
     for _ in range(args.warmup):
         cpu_rr_full(m, prm, npv_sample, ncores)
@@ -201,13 +212,14 @@ def impl_reference(args, rank):
         cpu_rr_full(m, prm, npv_sample, ncores)
     dt = time.perf_counter() - t
     value = args.steps * npv_sample * npt / dt
-    sample = (f"{npv_sample} of 8192 parameter vectors x {npt} times per step (oracle/rr_oracle.c "
+    sample = (f"all {npv_sample} parameter vectors x {npt} times per step (oracle/rr_oracle.c "
               f"rr_full restatement, OpenMP on {ncores} host threads, FP64)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "model points/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample_npv_per_step": npv_sample},
+            "config": {"workload": WORKLOAD, "npv_per_gpu": npv_sample, "npt": npt, "npb": 4, "nlc": 4,
+                       "nsamples": 1, "ld": "quadratic", "precision": "fp64"},
             "cpu_baseline": {"value": value, "unit": "model points/s", "cores": ncores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "model points/s", "h2d_bytes_per_step": 0,
@@ -255,7 +267,7 @@ def bench_model(model, prm, steps, torch, device):
     return t0.elapsed_time(t1) / steps, out
 
 
-def bench_c2(torch, device, steps=5):
+def bench_c2(torch, device, steps=5, n_oracle=256):
     from pytransit_gb300 import RoadRunnerModel
     data, prm = c2_workload()
     npv, npt = prm["p"].size, data["time"].size
@@ -266,12 +278,28 @@ def bench_c2(torch, device, steps=5):
         ms, out = bench_model(m, prm, steps if prec == "split" else 2, torch, device)
         res[prec] = (ms, out)
     dF = float((res["split"][1].double() - res["fp64"][1]).abs().max().item())
+    # a seeded subset of the population against the oracle (the reference's
+    # algorithm in FP64 C on the host cores), on the full C2 data
+    import oracle
+    sub = np.sort(np.random.default_rng(7).choice(npv, n_oracle, replace=False))
+    ref = oracle.OracleRoadRunner('power-2')
+    ref.set_data(**data)
+    t = time.perf_counter()
+    want = ref.evaluate(*(prm[n][sub] for n in ("k", "ldc", "t0", "p", "a", "i", "e", "w")))
+    t_oracle = time.perf_counter() - t
+    sub_t = torch.as_tensor(sub, device=device)
+    got64 = res["fp64"][1].index_select(0, sub_t).cpu().numpy()
+    got32 = res["split"][1].index_select(0, sub_t).double().cpu().numpy()
     pts = npv * npt
     return {"workload": f"{npv} pv x {npt} times (16 light curves, 30-min cadence, 10 supersamples, 4 passbands, "
                         "power-2 LD, eccentric)",
             "split_points_per_s": pts / (res["split"][0] / 1e3), "fp64_points_per_s": pts / (res["fp64"][0] / 1e3),
             "split_ms": res["split"][0], "fp64_ms": res["fp64"][0],
             "split_over_fp64": res["fp64"][0] / res["split"][0], "max_abs_dF_vs_fp64": dF,
+            "max_abs_dF_fp64_vs_oracle": float(np.abs(got64 - want).max()),
+            "max_abs_dF_split_vs_oracle": float(np.abs(got32 - want).max()),
+            "oracle_subset": f"{n_oracle} seeded parameter vectors x all {npt} times ({t_oracle:.1f} s on "
+                             f"{os.cpu_count()} host threads)",
             "timed": "RoadRunnerModel.evaluate(copy=False), CUDA events, parameters uploaded each call"}
 
 
@@ -373,88 +401,114 @@ def bench_eclipse(torch, device, data, prm, steps=3):
             "in_eclipse_fraction": float((out < k2 - 1e-12).double().mean().item())}
 
 
-def c4_requests(nreq, seed=4):
+class C4Mix:
     """The serving mix: npv log-uniform [1, 4096], npt log-uniform [500, 1e5],
     nsamples in {1, 5, 10}, LD in {quadratic, power-2, nonlinear}, 20 %
-    transmission-spectroscopy requests with 200 channels, k ~ U(0.09, 0.11)."""
-    rng = np.random.default_rng(seed)
-    T = 2459000.0
-    out = []
-    for j in range(nreq):
+    transmission-spectroscopy requests with 200 channels, k ~ U(0.09, 0.11);
+    2-min cadence from BJD 2459000.  Requests are views into shared pools
+    (times, radius ratios, LD coefficients), so that thousands of them cost
+    no host memory or generation time."""
+    LDC = {'quadratic': [0.35, 0.15], 'power-2': [0.6, 0.55], 'nonlinear': [0.5, -0.2, 0.6, -0.25]}
+
+    def __init__(self, seed=4):
+        pool = np.random.default_rng(1000 + seed)
+        self.rng = np.random.default_rng(seed)
+        self.time = 2459000.0 + np.arange(100000) * (2 / 1440)
+        self.k_ts = pool.uniform(0.09, 0.11, (2 * 4096, 200))
+        self.k_rr = pool.uniform(0.05, 0.15, (2 * 4096, 1))
+        self.ldc = {law: np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float64), (4096, 200, len(v))))
+                    for law, v in self.LDC.items()}
+
+    def request(self):
+        rng = self.rng
+        T = 2459000.0
         kind = 'ts' if rng.uniform() < 0.2 else 'rr'
         law = ['quadratic', 'power-2', 'nonlinear'][int(rng.integers(0, 3))]
         npv = int(np.exp(rng.uniform(0, np.log(4096))))
         npt = int(np.exp(rng.uniform(np.log(500), np.log(1e5))))
         ns = int(rng.choice([1, 5, 10]))
         cad = 2 / 1440
-        time_ = T + np.arange(npt) * cad
         npb = 200 if kind == 'ts' else 1
-        if law == 'nonlinear':
-            ldc = np.tile([0.5, -0.2, 0.6, -0.25], (npv, npb, 1))
-        elif law == 'power-2':
-            ldc = np.tile([0.6, 0.55], (npv, npb, 1))
-        else:
-            ldc = np.tile([0.35, 0.15], (npv, npb, 1))
-        k = rng.uniform(0.09, 0.11, (npv, npb)) if kind == 'ts' else rng.uniform(0.05, 0.15, (npv, 1))
+        o = int(rng.integers(0, 4096))
+        k = (self.k_ts if kind == 'ts' else self.k_rr)[o:o + npv]
         a = rng.uniform(3, 20, npv)
-        params = dict(k=k, ldc=ldc, t0=T + rng.normal(0, 1e-3, npv), p=rng.uniform(0.5, 15, npv), a=a,
-                      i=np.arccos(rng.uniform(0, 0.9, npv) / a), e=np.zeros(npv), w=np.zeros(npv))
-        data = dict(time=time_, nsamples=[ns], exptimes=[cad if ns > 1 else 0.0])
-        out.append((kind, law, data, params))
-    return out
+        params = dict(k=k, ldc=self.ldc[law][:npv, :npb], t0=T + rng.normal(0, 1e-3, npv),
+                      p=rng.uniform(0.5, 15, npv), a=a, i=np.arccos(rng.uniform(0, 0.9, npv) / a),
+                      e=np.zeros(npv), w=np.zeros(npv))
+        data = dict(time=self.time[:npt], nsamples=[ns], exptimes=[cad if ns > 1 else 0.0])
+        return kind, law, data, params
 
 
-def bench_serve(args):
-    """Poisson stream at --rate requests/s through RRServer (device-resident
-    results); p50/p99 latency, throughput; the plain FP64 path run per request
-    on the first requests for comparison."""
-    import threading
-    import torch
-    from pytransit_gb300 import RoadRunnerModel, TransmissionSpectroscopyModel
-    from pytransit_gb300.serving import RRServer
-    device = torch.device("cuda", 0)
-    torch.cuda.set_device(device)
-    reqs = c4_requests(args.nreq)
-    rng = np.random.default_rng(5)
-    gaps = rng.exponential(1.0 / args.rate, len(reqs))
-    srv = RRServer(hbm_budget=120e9, result='device', device=device)
-    # warm-up (tables, graph, allocator)
-    srv.submit(*c4_requests(2, seed=99)[0], keep_result=False).result()
-    done_t = {}
+def serve_run(srv, reqs, rate, seed=5):
+    """Submit reqs as a Poisson stream at `rate` requests/s; wait for all.
+    Returns the run's figures (latencies from submit to resolve)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, len(reqs))
+    st0 = dict(srv.stats.summary())
+    lat0 = len(srv.stats.latencies)
     futs = []
-    clk = ClockSampler(0).__enter__()
     t_start = time.perf_counter()
     t_next = t_start
-    for j, (r, gap) in enumerate(zip(reqs, gaps)):
+    for r, gap in zip(reqs, gaps):
         t_next += gap
         while time.perf_counter() < t_next:
             time.sleep(0.0001)
-        f = srv.submit(*r, keep_result=False)
-        f.add_done_callback(lambda fut, j=j: done_t.__setitem__(j, time.perf_counter()))
-        futs.append(f)
-    ok = 0
-    points = 0
-    rejected = set()
-    for j, f in enumerate(futs):
+        futs.append((time.perf_counter(), srv.submit(*r, keep_result=False)))
+    t_arrivals = time.perf_counter()
+    load_end = srv.load()
+    points, done, rejected, failed = 0, [], 0, 0
+    for t_sub, f in futs:
         try:
             points += f.result()
-            ok += 1
+            done.append(t_sub)
         except MemoryError:
-            rejected.add(j)
-        futs[j] = None
+            rejected += 1
+        except Exception:
+            failed += 1
     t_end = time.perf_counter()
-    clk.__exit__(None, None, None)
-    clocks = clk.summary()
-    stats = srv.stats.summary()
-    srv.close()
-    # the same requests one at a time through the drop-in models (no batching):
-    # the plain FP64 path, and the split path for reference
-    per_req = {}
-    models = {}
+    st = srv.stats.summary()
+    lat = np.array(srv.stats.latencies[lat0:])
+    dts = np.array(srv.stats.done_times[lat0:])
+    n = len(lat)
+    half = n // 2
+    p99 = lambda x: float(np.percentile(x, 99)) if len(x) else None
+    in_window = int((dts <= t_arrivals).sum()) if n else 0
+    wall_arr = t_arrivals - t_start
+    return {"offered_req_per_s": rate, "requests": len(reqs), "completed": n, "rejected": rejected,
+            "failed": failed, "arrival_window_s": wall_arr, "wall_s": t_end - t_start,
+            "achieved_req_per_s": n / (t_end - t_start),
+            "completed_in_window_req_per_s": in_window / wall_arr,
+            "points_per_s": points / (t_end - t_start),
+            "latency_p50_s": float(np.percentile(lat, 50)) if n else None, "latency_p99_s": p99(lat),
+            "latency_mean_s": float(lat.mean()) if n else None,
+            "latency_p99_first_half_s": p99(lat[:half]), "latency_p99_second_half_s": p99(lat[half:]),
+            "queued_at_end_of_arrivals": load_end["queued"], "active_at_end_of_arrivals": load_end["active"],
+            "admitted_bytes_at_end_of_arrivals": load_end["admitted_bytes"],
+            "steps": st["steps"] - st0["steps"], "bypassed": st["bypassed"] - st0["bypassed"]}
+
+
+def sustained(run):
+    """Achieved = offered, the queue empty when arrivals stop, p99 flat."""
+    a, b = run["latency_p99_first_half_s"], run["latency_p99_second_half_s"]
+    return (run["achieved_req_per_s"] >= 0.97 * run["offered_req_per_s"] and
+            run["queued_at_end_of_arrivals"] <= max(10, 0.01 * run["requests"]) and
+            a is not None and b is not None and b <= 1.5 * a + 0.005)
+
+
+def per_request_paths(reqs, torch, device, nsample):
+    """The first nsample requests one at a time through the drop-in models
+    (no batching): the plain FP64 path, and the split path beside it.  A
+    request larger than the server's budget (which the server rejects) or
+    whose FP64 output would take more than 100 GB is skipped."""
+    from pytransit_gb300 import RoadRunnerModel, TransmissionSpectroscopyModel
+    out, models = {}, {}
     for prec in ("fp64", "split"):
-        n_plain, t_plain, pts_plain = 0, 0.0, 0
-        for j, (kind, law, data, params) in enumerate(reqs[:args.plain_sample]):
-            if j in rejected:          # larger than the HBM budget: not served either
+        n, t_tot, pts, skipped = 0, 0.0, 0, 0
+        for kind, law, data, params in reqs[:nsample]:
+            npv, npt = params["p"].size, data["time"].size
+            npb = params["k"].shape[1] if kind == 'ts' else 1
+            if npv * npb * npt * 4 > 120e9 or npv * npb * npt * 8 > 100e9:
+                skipped += 1
                 continue
             key = (kind, law, prec)
             if key not in models:
@@ -471,31 +525,75 @@ def bench_serve(args):
                         params["i"], params["e"], params["w"])
             torch.cuda.synchronize(device)
             t = time.perf_counter()
-            out = m.evaluate(*argv, copy=False)
+            res = m.evaluate(*argv, copy=False)
             torch.cuda.synchronize(device)
-            t_plain += time.perf_counter() - t
-            pts_plain += out.numel()
-            n_plain += 1
-            del out
-        per_req[prec] = dict(requests=n_plain, points_per_s=pts_plain / max(t_plain, 1e-9), wall_s=t_plain)
+            t_tot += time.perf_counter() - t
+            pts += res.numel()
+            n += 1
+            del res
+        out[prec] = dict(requests=n, skipped=skipped, points_per_s=pts / max(t_tot, 1e-9), wall_s=t_tot)
     del models
+    torch.cuda.empty_cache()
+    return out
+
+
+def serve_suite(torch, device, rate=2000.0, duration_s=5.0, probe_s=2.5, max_probes=3, plain_sample=200):
+    """The serving leg: the C4 mix as a Poisson stream at `rate` for
+    `duration_s` through RRServer (split precision, device-resident results,
+    120 GB budget); then shorter runs at other rates to find the highest one
+    the server sustains (upwards in 1.5x steps if `rate` is sustained, else
+    downwards); then the plain FP64 path on the same requests one at a time."""
+    from pytransit_gb300.serving import RRServer
+    mix = C4Mix(4)
+    srv = RRServer(hbm_budget=120e9, result='device', device=device)
+    srv.submit(*C4Mix(99).request(), keep_result=False).result()      # warm-up: tables, graph, arena
+    reqs = [mix.request() for _ in range(int(rate * duration_s))]
+    with ClockSampler(0) as clk:
+        main_run = serve_run(srv, reqs, rate)
+    clocks = clk.summary()
+    probes = []
+    ok = sustained(main_run)
+    best = rate if ok else None
+    r = rate
+    for j in range(max_probes):
+        r = r * 1.5 if ok else r / 1.5
+        run = serve_run(srv, [mix.request() for _ in range(int(r * probe_s))], r, seed=6 + j)
+        probes.append({k: run[k] for k in ("offered_req_per_s", "achieved_req_per_s", "latency_p50_s",
+                                            "latency_p99_s", "latency_p99_first_half_s",
+                                            "latency_p99_second_half_s", "queued_at_end_of_arrivals",
+                                            "points_per_s")})
+        good = sustained(run)
+        probes[-1]["sustained"] = good
+        if good:
+            best = r if best is None else max(best, r)
+        if good != ok:
+            break
+    srv.close()
+    plain = per_request_paths(reqs, torch, device, plain_sample)
+    res = dict(main_run)
+    res.update({
+        "workload": f"C4 mix, Poisson arrivals at {rate:g} req/s for {duration_s:g} s ({len(reqs)} requests): npv "
+                    "log-U[1,4096], npt log-U[500,1e5], nsamples {1,5,10}, LD {quadratic, power-2, nonlinear}, "
+                    "20% TS with 200 channels; split precision; results kept on the device; HBM budget 120 GB",
+        "sustained": ok, "max_sustained_req_per_s": best, "rate_probes": probes,
+        "plain_fp64_per_request": dict(plain["fp64"], sample=f"the first {plain_sample} requests of the stream one "
+                                       "at a time, RoadRunnerModel / TransmissionSpectroscopyModel precision='fp64', "
+                                       "copy=False, data upload included"),
+        "split_per_request": dict(plain["split"], sample="the same requests one at a time, precision='split'"),
+        "served_over_plain_fp64": main_run["points_per_s"] / plain["fp64"]["points_per_s"],
+        "clocks": clocks})
+    return res
+
+
+def bench_serve(args):
+    """--workload serve: the serving leg alone, one JSON line."""
+    import torch
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    res = serve_suite(torch, device, rate=args.rate, duration_s=args.serve_s, plain_sample=args.plain_sample)
     line = {"metric": "served model points/s (Poisson request stream); p50/p99 latency",
-            "value": points / (t_end - t_start), "unit": "model points/s", "n_gpus": 1,
-            "higher_is_better": True, "data": "synthetic (seeded)",
-            "config": {"workload": f"{len(reqs)} requests, Poisson arrivals at {args.rate} req/s; npv log-U[1,4096], "
-                                   "npt log-U[500,1e5], nsamples {1,5,10}, LD {quadratic, power-2, nonlinear}, 20% TS "
-                                   "with 200 channels; split precision; results kept on the device; HBM budget 120 GB"},
-            "latency_p50_s": stats["p50_s"], "latency_p99_s": stats["p99_s"], "latency_mean_s": stats["mean_s"],
-            "completed": stats["completed"], "rejected": stats["rejected"], "steps": stats["steps"],
-            "wall_s": t_end - t_start, "offered_req_per_s": args.rate,
-            "achieved_req_per_s": stats["completed"] / (t_end - t_start),
-            "peak_admitted_bytes": stats["peak_hbm_bytes"],
-            "clocks": clocks,
-            "plain_fp64_per_request": dict(per_req["fp64"], sample="the same requests one at a time (data upload "
-                                           "included), RoadRunnerModel / TransmissionSpectroscopyModel "
-                                           "precision='fp64', copy=False"),
-            "served_over_plain_fp64": (points / (t_end - t_start)) / per_req["fp64"]["points_per_s"],
-            "split_per_request": dict(per_req["split"], sample="the same requests one at a time, precision='split'")}
+            "value": res["points_per_s"], "unit": "model points/s", "n_gpus": 1, "higher_is_better": True,
+            "data": "synthetic (seeded)", "config": {"workload": res["workload"]}, **res}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -509,13 +607,16 @@ def main():
     ap.add_argument("--npv", type=int, default=8192)
     ap.add_argument("--npt", type=int, default=19700)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-size check against the oracle")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg of the default line")
     ap.add_argument("--no-extra", action="store_true", help="skip the precision and gradient workloads")
     ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "ts", "serve"],
                     help="c1: the default line; c2 / c3 / ts: the precision / gradient / transmission-spectroscopy "
                          "workload alone; serve: Poisson stream")
-    ap.add_argument("--rate", type=float, default=2000.0)
-    ap.add_argument("--nreq", type=int, default=300)
-    ap.add_argument("--plain-sample", type=int, default=100000)
+    ap.add_argument("--rate", type=float, default=2000.0, help="serving leg: offered requests/s")
+    ap.add_argument("--serve-s", type=float, default=5.0, help="serving leg: seconds of arrivals at --rate")
+    ap.add_argument("--plain-sample", type=int, default=200,
+                    help="serving leg: requests run one at a time through the plain FP64 path")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -639,6 +740,10 @@ def main():
     torch.cuda.synchronize(device)
     dF = float((flux32[:, :npt].double() - flux64).abs().max().item())
     in_transit = float((flux64 < 1.0).double().mean().item())
+    # host copies of both results, checked against the oracle's FP64 flux of the
+    # whole population after the CPU-baseline leg has computed it
+    host64 = flux64.cpu().numpy() if rank == 0 and world == 1 and not args.no_parity else None
+    host32 = flux32[:, :npt].cpu().numpy() if host64 is not None else None
     # independent cross-check: the Mandel & Agol quadratic model on the same
     # orbit layer as the FP64 RoadRunner step just run (its workspace)
     ma_check = None
@@ -706,7 +811,11 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "flux_split_kernel", "kernel_ms": kern_avg_s * 1e3,
-                     "bytes_alg_per_launch": bytes_alg},
+                     "bytes_alg_per_launch": bytes_alg,
+                     # the same kernel time against the DRAM bytes ncu measured for it: part of the
+                     # algorithmic bytes (LD tables, the output's tail) are served by or stay in L2
+                     "achieved_dram": traffic / kern_avg_s / 1e9 if traffic else None,
+                     "frac_dram": traffic / kern_avg_s / 1e9 / peak if traffic else None},
         "clocks": clocks,
         # per step: the fused prologue (LD tables, LD means, orbit records) and the flux kernel
         "gpu_launches": 2 * args.steps,
@@ -716,8 +825,25 @@ def main():
         line["c3_gradient"] = bench_c3(torch, device)
         line["ts"] = bench_ts(torch, device)
         line["eclipse"] = bench_eclipse(torch, device, data, prm)
+    if rank == 0 and world == 1 and not args.no_serve:
+        del flux64, flux32, ws32, ws64
+        torch.cuda.empty_cache()
+        line["serve"] = serve_suite(torch, device, rate=args.rate, duration_s=args.serve_s,
+                                    plain_sample=args.plain_sample)
+    keep = {}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = run_cpu_baseline(data, prm)
+        line["cpu_baseline"] = run_cpu_baseline(data, prm, keep=keep)
+    if host64 is not None:
+        if "flux" not in keep:
+            keep["flux"] = cpu_rr_full(cpu_oracle_model(data), prm, npv, os.cpu_count() or 1)
+        want = keep.pop("flux")
+        line["parity_vs_oracle"] = {
+            "max_abs_dF_fp64_vs_oracle": float(np.abs(host64 - want).max()),
+            "max_abs_dF_split_vs_oracle": float(np.abs(host32.astype(np.float64) - want).max()),
+            "points": int(want.size), "bound_fp64": 1e-9, "bound_split": 1e-6,
+            "what": "the whole workload (all parameter vectors x all times): the GPU's FP64 and split results "
+                    "against the oracle's FP64 rr_full restatement (oracle/rr_oracle.c) on the host cores"}
+        del want, host64, host32
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

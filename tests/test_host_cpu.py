@@ -173,3 +173,27 @@ def test_bench_reads_the_profiled_traffic_and_peak():
     assert 3.0 < bpp < 4.5, bpp
     peak, kind = bench.measured_peaks()
     assert peak > 1000 and kind in ("measured", "fallback")
+
+
+def test_bench_serving_mix_and_sustained_rule():
+    """The serving mix draws the configured distributions (20 % TS requests
+    with 200 channels, npv and npt within their ranges) from shared pools, and
+    a run counts as sustained only when it keeps up with the offered rate."""
+    import bench
+    mix = bench.C4Mix(4)
+    reqs = [mix.request() for _ in range(2000)]
+    ts = [r for r in reqs if r[0] == 'ts']
+    assert 0.17 < len(ts) / len(reqs) < 0.23
+    for kind, law, data, params in reqs[:200]:
+        npv, npt = params['p'].size, data['time'].size
+        assert 1 <= npv <= 4096 and 500 <= npt <= 100000
+        assert params['k'].shape == (npv, 200 if kind == 'ts' else 1)
+        assert params['ldc'].shape[:2] == (npv, 200 if kind == 'ts' else 1)
+        assert data['nsamples'][0] in (1, 5, 10)
+        assert np.all((params['k'] >= (0.09 if kind == 'ts' else 0.05)) & (params['k'] <= 0.15))
+    run = dict(offered_req_per_s=2000, achieved_req_per_s=1990, requests=10000, queued_at_end_of_arrivals=3,
+               latency_p99_first_half_s=0.02, latency_p99_second_half_s=0.021)
+    assert bench.sustained(run)
+    assert not bench.sustained(dict(run, achieved_req_per_s=1700))
+    assert not bench.sustained(dict(run, queued_at_end_of_arrivals=500))
+    assert not bench.sustained(dict(run, latency_p99_second_half_s=0.2))
