@@ -316,22 +316,79 @@ def bench_ts(torch, device, steps=5, npv=64, npb=200, npt=19700):
                t0=T + 13.7 + rng.normal(0, 1e-3, npv), p=rng.uniform(0.5, 15.0, npv), a=a,
                i=np.arccos(rng.uniform(0.0, 0.9, npv) / a), e=np.zeros(npv), w=np.zeros(npv))
     res = {}
+    models = {}
     for prec in ("split", "fp64"):
-        m = TSModel('quadratic', precision=prec, device=device)
+        m = models[prec] = TSModel('quadratic', precision=prec, device=device)
         m.set_data(time_)
         res[prec] = bench_model(m, prm, steps if prec == "split" else 2, torch, device)
     dF = float((res["split"][1].double() - res["fp64"][1]).abs().max().item())
     pts = npv * npb * npt
     out_bytes = pts * 4
     peak, _ = measured_peaks()
+    # host time of one evaluate() call (the calls are issued back to back;
+    # the GPU work of a call overlaps the host work of the next)
+    m = models["split"]
+    argv = (prm["k"], prm["ldc"], prm["t0"], prm["p"], prm["a"], prm["i"], prm["e"], prm["w"])
+    torch.cuda.synchronize(device)
+    t = time.perf_counter()
+    for _ in range(steps):
+        m.evaluate(*argv, copy=False)
+    host_ms = (time.perf_counter() - t) / steps * 1e3
+    torch.cuda.synchronize(device)
+    # the same model through the C ABI with its inputs resident in HBM:
+    # the fused prologue and the flux kernel per step, CUDA events
+    from pytransit_gb300 import _lib
+    L = _lib.lib()
+    P = _lib.ptr
+    tb, dd = m._device_tables(device), m._device_data(device)
+    dev = {n: torch.as_tensor(np.ascontiguousarray(prm[n], dtype=np.float64)).to(device)
+           for n in ("k", "ldc", "t0", "p", "a", "i", "e", "w")}
+    ldf = (npt + 3) // 4 * 4
+    flux = torch.empty((npv, npb, ldf), dtype=torch.float32, device=device)
+    wsb = L.rr_ts_workspace_bytes(1, npv, npb, m.ng)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device)
+    sp = _lib.stream_ptr(device)
+    orbit = tuple(P(dev[n]) for n in ("k", "t0", "p", "a", "i", "e", "w"))
+
+    def step(ev=None):
+        _lib.check(L.rr_ts_prepare_split_ld(m.ld_law, P(dev["ldc"]), 2, P(tb["mu"]), dd["t_ref"], dd["t_absmax"],
+                                            *orbit, npv, npb, 0.0, m.ng, m.ze.size, P(tb["ze"]), P(ws), wsb, sp))
+        if ev is not None:
+            ev[0].record(stream)
+        _lib.check(L.rr_ts_flux_split(P(dd["times_ff"]), npt, npv, npb, 1, 0.0, m.ng, m.dg, P(ws), P(flux), ldf, sp))
+        if ev is not None:
+            ev[1].record(stream)
+
+    for _ in range(3):
+        step()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    t0.record(stream)
+    for j in range(steps):
+        step(evs[j])
+    t1.record(stream)
+    torch.cuda.synchronize(device)
+    dev_ms = t0.elapsed_time(t1) / steps
+    flux_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    dF_dev = float((flux[:, :, :npt].double() - res["fp64"][1]).abs().max().item())
     return {"workload": f"TSModel, {npv} pv x {npb} channels x {npt} times (2-min cadence), quadratic LD, nsamples=1",
             "split_points_per_s": pts / (res["split"][0] / 1e3), "fp64_points_per_s": pts / (res["fp64"][0] / 1e3),
             "split_ms": res["split"][0], "fp64_ms": res["fp64"][0],
             "split_over_fp64": res["fp64"][0] / res["split"][0], "max_abs_dF_vs_fp64": dF,
             "split_output_gbs": out_bytes / (res["split"][0] / 1e3) / 1e9,
             "split_output_frac_of_hbm": out_bytes / (res["split"][0] / 1e3) / 1e9 / peak,
+            "host_ms_per_call": host_ms,
             "timed": "TSModel.evaluate(copy=False) (prologue, 2D LD tables and flux), CUDA events, "
-                     "parameters uploaded each call"}
+                     "parameters uploaded each call",
+            "device_resident": {
+                "ms_per_step": dev_ms, "points_per_s": pts / (dev_ms / 1e3),
+                "output_frac_of_hbm": out_bytes / (dev_ms / 1e3) / 1e9 / peak,
+                "flux_kernel_ms": flux_ms, "flux_kernel_frac_of_hbm": out_bytes / (flux_ms / 1e3) / 1e9 / peak,
+                "max_abs_dF_vs_fp64": dF_dev,
+                "timed": "rr_ts_prepare_split_ld + rr_ts_flux_split through the C ABI, inputs in HBM, CUDA events"}}
 
 
 def bench_c3(torch, device, steps=3):
@@ -553,10 +610,12 @@ def serve_suite(torch, device, rate=2000.0, duration_s=5.0, probe_s=2.5, max_pro
     clocks = clk.summary()
     probes = []
     ok = sustained(main_run)
-    best = rate if ok else None
-    r = rate
+    lo, hi = (rate, None) if ok else (None, rate)     # highest sustained / lowest not sustained so far
     for j in range(max_probes):
-        r = r * 1.5 if ok else r / 1.5
+        if lo is not None and hi is not None:
+            r = (lo * hi) ** 0.5                        # bisect (geometrically) once bracketed
+        else:
+            r = lo * 1.5 if hi is None else hi / 1.5
         run = serve_run(srv, [mix.request() for _ in range(int(r * probe_s))], r, seed=6 + j)
         probes.append({k: run[k] for k in ("offered_req_per_s", "achieved_req_per_s", "latency_p50_s",
                                             "latency_p99_s", "latency_p99_first_half_s",
@@ -565,9 +624,10 @@ def serve_suite(torch, device, rate=2000.0, duration_s=5.0, probe_s=2.5, max_pro
         good = sustained(run)
         probes[-1]["sustained"] = good
         if good:
-            best = r if best is None else max(best, r)
-        if good != ok:
-            break
+            lo = r if lo is None else max(lo, r)
+        else:
+            hi = r if hi is None else min(hi, r)
+    best = lo
     srv.close()
     plain = per_request_paths(reqs, torch, device, plain_sample)
     res = dict(main_run)
@@ -575,7 +635,8 @@ def serve_suite(torch, device, rate=2000.0, duration_s=5.0, probe_s=2.5, max_pro
         "workload": f"C4 mix, Poisson arrivals at {rate:g} req/s for {duration_s:g} s ({len(reqs)} requests): npv "
                     "log-U[1,4096], npt log-U[500,1e5], nsamples {1,5,10}, LD {quadratic, power-2, nonlinear}, "
                     "20% TS with 200 channels; split precision; results kept on the device; HBM budget 120 GB",
-        "sustained": ok, "max_sustained_req_per_s": best, "rate_probes": probes,
+        "sustained": ok, "max_sustained_req_per_s": best, "lowest_unsustained_req_per_s": hi,
+        "rate_probes": probes,
         "plain_fp64_per_request": dict(plain["fp64"], sample=f"the first {plain_sample} requests of the stream one "
                                        "at a time, RoadRunnerModel / TransmissionSpectroscopyModel precision='fp64', "
                                        "copy=False, data upload included"),

@@ -197,6 +197,42 @@ int rr_ts_f64(const double *times, int npt, const double *k, const double *t0, c
               int nsamples0, double exptime0, const double *ldp, const double *istar, const double *weights,
               int nk, int ng, int nz, double dk, double kmin, double kmax, double dg, const double *z_edges,
               void *workspace, size_t workspace_bytes, double *flux, int ldflux, void *stream);
+/* The two halves of rr_ts_split (for callers that keep the per-pv tables
+ * between calls, such as the serving loop): rr_ts_prepare_split writes the
+ * per-pv records, the channel records and the LD means into the workspace
+ * (tsmodel_serial's per-pv prologue, model_trspec.py:36-66); rr_ts_flux_split
+ * evaluates the light curves from them (model_trspec.py:72-93).
+ * rr_ts_tables gives the addresses of those tables inside the workspace. */
+int rr_ts_prepare_split(double t_ref, double t_absmax, const double *k, const double *t0, const double *p,
+                        const double *a, const double *inc, const double *e, const double *w, int npv, int npb,
+                        double exptime0, const float *ldp, const float *istar, const float *weights, int nk, int ng,
+                        int nz, double dk, double kmin, double kmax, const double *z_edges, void *workspace,
+                        size_t workspace_bytes, void *stream);
+int rr_ts_flux_split(const float *times_ff, int npt, int npv, int npb, int nsamples0, double exptime0, int ng,
+                     double dg, const void *workspace, float *flux, int ldflux, void *stream);
+/* rr_ts_flux_split for the parameter vectors [pv0, pv1) of a workspace
+ * prepared for npv: flux holds their rows only, flux[pv1 - pv0, npb, ldflux]. */
+int rr_ts_flux_split_range(const float *times_ff, int npt, int npv, int npb, int nsamples0, double exptime0, int ng,
+                           double dg, const void *workspace, int pv0, int pv1, float *flux, int ldflux, void *stream);
+void rr_ts_tables(void *workspace, int split, int npv, int npb, int ng, const void **orb, const void **ch,
+                  const void **ldm);
+/* The prologue for a named law with the default 2D table (TSModel.evaluate
+ * with a string ldmodel, tsmodel.py:46-130: evaluate_ld / evaluate_ldi or the
+ * 200-point trapezoid, then tsmodel_serial's per-pv prologue,
+ * model_trspec.py:36-66), one launch: ldc[npv, npb, npar] on the mu grid
+ * mu[nz] instead of ldp / istar.  rr_ts_flux_f64 is the plain path's flux
+ * half (model_trspec.py:72-93). */
+int rr_ts_prepare_split_ld(int law, const double *ldc, int npar, const double *mu, double t_ref, double t_absmax,
+                           const double *k, const double *t0, const double *p, const double *a, const double *inc,
+                           const double *e, const double *w, int npv, int npb, double exptime0, int ng, int nz,
+                           const double *z_edges, void *workspace, size_t workspace_bytes, void *stream);
+int rr_ts_prepare_f64_ld(int law, const double *ldc, int npar, const double *mu, const double *k, const double *t0,
+                         const double *p, const double *a, const double *inc, const double *e, const double *w,
+                         int npv, int npb, double exptime0, int ng, int nz, const double *z_edges, void *workspace,
+                         size_t workspace_bytes, void *stream);
+int rr_ts_flux_f64(const double *times, int npt, const double *t0, const double *p, int npv, int npb, int nsamples0,
+                   double exptime0, int ng, double dg, const void *workspace, double *flux, int ldflux,
+                   void *stream);
 /* Same, split precision (times_ff and t_ref/t_absmax as rr_full_split). */
 int rr_ts_split(const float *times_ff, double t_ref, double t_absmax, int npt, const double *k,
                 const double *t0, const double *p, const double *a, const double *inc, const double *e,
@@ -295,10 +331,16 @@ int rr_lpf_map(const double *pv, int npv, int ldpv, int npb, int ld_start, doubl
 
 /* ---- serving: many requests in one persistent launch ---------------------- */
 
-/* One request of the serving loop (all pointers on the device): the data of
- * rr_time_split (times_ff) and set_data (lcids), the tables written by
- * rr_prepare_split (rr_full_split_tables gives their addresses inside the
- * workspace) and the request's output flux[npv, ldflux]. */
+/* One request of the serving loop (all pointers on the device).
+ * kind 0, a RoadRunner request: the data of rr_time_split (times_ff) and
+ * set_data (lcids), the tables written by rr_prepare_split
+ * (rr_full_split_tables gives their addresses inside the workspace) and the
+ * output flux[npv, ldflux].
+ * kind 1, a transmission-spectroscopy request: times_ff, the tables written by
+ * rr_ts_prepare_split[_ld] (rr_ts_tables: orb32 <- the per-pv records, lc32 <-
+ * the channel records, ldm <- the LD means), npb channels, nsamples0,
+ * exptime0 and dg, and the output flux[npv, npb, ldflux]; lcids and nlc are
+ * not used. */
 typedef struct {
   const float *times_ff;
   const int32_t *lcids;
@@ -307,8 +349,10 @@ typedef struct {
   const float *ldm;
   float *flux;
   int64_t ldflux;
-  int32_t npt, npv, nlc, npb, ng, pad0;
-  float inv_dg, pad1;
+  int32_t npt, npv, nlc, npb, ng, kind;
+  float inv_dg, exptime0;
+  double dg;
+  int32_t nsamples0, pad;
 } rr_serve_request;
 
 /* A unit of work: parameter vectors [pv0, pv1) x 128-point tiles [tile0, tile1) of request req. */
@@ -322,7 +366,9 @@ void rr_full_split_tables(void *workspace, int npv, int npb, int nlc, int nep, i
                           const float **lc32, const float **ldm);
 /* No counterpart in the reference (serving layer): nblocks persistent blocks
  * take the items items[0 .. *nitems) from *counter (set to 0 beforehand) and
- * write every covered flux value of the requests; returns at launch. */
+ * write every covered flux value of the requests (every channel row of a
+ * transmission-spectroscopy request; its items span at most 32 tiles);
+ * returns at launch. */
 int rr_serve_flux_split(const rr_serve_request *reqs, const rr_serve_item *items, const int *nitems, int *counter,
                         int nblocks, void *stream);
 

@@ -63,6 +63,16 @@ def _sig(L):
                 _vp, _vp, _sz, _vp, _i, _vp]
     L.rr_ts_f64.argtypes = [_vp, _i] + _ts_tail
     L.rr_ts_split.argtypes = [_vp, _d, _d, _i] + _ts_tail
+    _orbit = [_vp] * 7
+    L.rr_ts_prepare_split.argtypes = [_d, _d] + _orbit + [_i, _i, _d, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _vp,
+                                                          _vp, _sz, _vp]
+    L.rr_ts_prepare_split_ld.argtypes = [_i, _vp, _i, _vp, _d, _d] + _orbit + [_i, _i, _d, _i, _i, _vp, _vp, _sz,
+                                                                              _vp]
+    L.rr_ts_prepare_f64_ld.argtypes = [_i, _vp, _i, _vp] + _orbit + [_i, _i, _d, _i, _i, _vp, _vp, _sz, _vp]
+    L.rr_ts_flux_split.argtypes = [_vp, _i, _i, _i, _i, _d, _i, _d, _vp, _vp, _i, _vp]
+    L.rr_ts_flux_f64.argtypes = [_vp, _i, _vp, _vp, _i, _i, _i, _d, _i, _d, _vp, _vp, _i, _vp]
+    L.rr_ts_tables.argtypes = [_vp, _i, _i, _i, _i, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]
+    L.rr_ts_tables.restype = None
     for name, args in _EXTRA_SIGNATURES.items():
         if hasattr(L, name):
             getattr(L, name).argtypes = args[0]

@@ -7,6 +7,7 @@
 
 #include "rr_device.cuh"
 #include "rr_internal.h"
+#include "rr_ts.cuh"
 
 namespace rr {
 
@@ -1075,10 +1076,15 @@ __global__ void __launch_bounds__(FLUX_NW * 32) flux_split_kernel(FluxSplitArgs 
 // counter and runs split_pv_tiles for it with that request's tables; the
 // item list is complete at launch, so no block ever waits for work.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(SPLIT_WARPS * 32)
+__global__ void __launch_bounds__(SPLIT_WARPS * 32, 3)
 serve_split_kernel(const rr_serve_request* __restrict__ reqs, const rr_serve_item* __restrict__ items,
                    const int* __restrict__ nitems_p, int* __restrict__ counter) {
-  __shared__ WarpList lists[SPLIT_WARPS];
+  // the per-warp lists of the RoadRunner tiles and the tile state of the
+  // transmission-spectroscopy tiles share the block's shared memory
+  __shared__ union ServeSmem {
+    WarpList lists[SPLIT_WARPS];
+    TsSmem<float> ts;
+  } U;
   __shared__ __align__(16) float recs[ORB32 + LC_SMEM * LC32];
   __shared__ int s_item;
   const int nitems = *nitems_p;
@@ -1090,6 +1096,23 @@ serve_split_kernel(const rr_serve_request* __restrict__ reqs, const rr_serve_ite
     if (it >= nitems) return;
     const rr_serve_item w = items[it];
     const rr_serve_request& r = reqs[w.req];
+    if (r.kind == 1) {
+      // transmission spectroscopy (rr_ts.cuh): items span at most 32 tiles
+      TsArgs<float> T{};
+      T.times_ff = reinterpret_cast<const float2*>(r.times_ff);
+      T.orb = r.orb32; T.ch = r.lc32; T.ldm = r.ldm; T.flux = r.flux;
+      T.ldflux = r.ldflux; T.npt = r.npt; T.npb = r.npb; T.ng = r.ng; T.nsamples0 = r.nsamples0;
+      T.exptime0 = (double)r.exptime0; T.dg = r.dg;
+      for (int pv = w.pv0; pv < w.pv1; ++pv) {
+        __syncthreads();   // the previous pv's record is consumed
+        if (threadIdx.x < TS_ORB) recs[threadIdx.x] = __ldg(r.orb32 + (size_t)pv * TS_ORB + threadIdx.x);
+        __syncthreads();
+        ts_range<float, true>(T, pv, w.tile0, w.tile1, recs, U.ts);
+      }
+      __syncthreads();
+      continue;
+    }
+    WarpList* lists = U.lists;
     FluxSplitArgs A{};
     A.times_ff = reinterpret_cast<const float2*>(r.times_ff);
     A.lcids = r.lcids;
@@ -1318,9 +1341,9 @@ int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, in
   fa.npt = npt; fa.npv = npv; fa.npb = npb; fa.nlc = nlc; fa.ng = ng; fa.ldflux = ldflux;
   fa.inv_dg = (float)(1.0 / dg); fa.flux = flux;
   // tile ranges of FLUX_CHUNK tiles, shorter when the launch would otherwise
-  // have fewer than about four blocks per resident warp slot (152 SMs x 32)
+  // have fewer than about four blocks per resident warp slot (SMs x 32)
   const int ntiles = (npt + WARP_TILE - 1) / WARP_TILE;
-  long long chunk = (long long)ntiles * npv / (4LL * 152 * 32);
+  long long chunk = (long long)ntiles * npv / (4LL * sm_count() * 32);
   chunk = chunk < 1 ? 1 : (chunk > FLUX_CHUNK ? FLUX_CHUNK : chunk);
   const int bx = (int)((ntiles + chunk - 1) / chunk);
   dim3 fg((unsigned)bx, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);

@@ -23,6 +23,10 @@ void launch_ldm_f64(const double* ldp, int npv, int npb, int nz, const double* k
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Multiprocessor count of the current device (queried once per device), for
+// launch shapes.
+int sm_count();
+
 // Bump allocator over a caller-owned workspace (256-byte aligned pieces).
 struct Carve {
   char* base;

@@ -15,6 +15,18 @@ void set_cuda_error(cudaError_t e, const char* where) {
   snprintf(g_last_error, sizeof(g_last_error), "%s: %s", where, cudaGetErrorString(e));
 }
 
+int sm_count() {
+  constexpr int kMaxDev = 64;
+  static int cached[kMaxDev] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 152;
+  if (dev < kMaxDev && cached[dev] > 0) return cached[dev];
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 152;
+  if (dev < kMaxDev) cached[dev] = n;
+  return n;
+}
+
 int check_launch(const char* where) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -96,33 +108,35 @@ constexpr int MAX_LDPAR = 16;
 constexpr int NTRAP = 200;
 
 // evaluate_ld + evaluate_ldi (ldmodels.py:143-174) or the 200-point trapezoid
-// of rrmodel.py:222-227, one thread per (pv, pb).
+// of rrmodel.py:222-227, one warp per (pv, pb): lanes over the mu grid, and
+// over the trapezoid's intervals with a warp sum.
 template <typename R>
-__global__ void ld_tables_kernel(int law, const double* __restrict__ ldc, int npvpb, int npar,
-                                 const double* __restrict__ mu, int nz, R* __restrict__ ldp,
-                                 R* __restrict__ istar) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= npvpb) return;
+__global__ void __launch_bounds__(128) ld_tables_kernel(int law, const double* __restrict__ ldc, int npvpb, int npar,
+                                                        const double* __restrict__ mu, int nz, R* __restrict__ ldp,
+                                                        R* __restrict__ istar) {
+  const int j = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (j >= npvpb) return;   // warp-uniform
   R pv[MAX_LDPAR];
   for (int i = 0; i < npar; ++i) pv[i] = (R)ldc[(size_t)j * npar + i];
-  for (int i = 0; i < nz; ++i) ldp[(size_t)j * nz + i] = ld_value<R>(law, (R)mu[i], pv, npar);
+  for (int i = lane; i < nz; i += 32) ldp[(size_t)j * nz + i] = ld_value<R>(law, (R)mu[i], pv, npar);
   R is;
   if (!ld_integral<R>(law, pv, is)) {
-    // 2*pi*trapezoid(z*I(mu(z)), z), mu = linspace(1, 0, 200), z = sqrt(1 - mu^2)
-    R s = R(0), z0 = R(0), y0 = R(0);
-    for (int i = 0; i < NTRAP; ++i) {
+    // 2*pi*trapezoid(z*I(mu(z)), z), mu = linspace(1, 0, 200), z = sqrt(1 - mu^2);
+    // lane l takes the intervals i = l, l + 32, ...
+    R s = R(0);
+    for (int i = lane + 1; i < NTRAP; i += 32) {
       // (n-1-i)/(n-1): exactly 1 and 0 at the ends (a select of the end value
       // was not honoured by the nvcc 13.0 -O3 build, leaving mu = -1.5e-17)
-      R m = R(NTRAP - 1 - i) / R(NTRAP - 1);
-      R z = sqrt(R(1) - m * m);
-      R y = z * ld_value<R>(law, m, pv, npar);
-      if (i > 0) s += (z - z0) * (y + y0) / R(2);
-      z0 = z;
-      y0 = y;
+      const R m0 = R(NTRAP - i) / R(NTRAP - 1), m1 = R(NTRAP - 1 - i) / R(NTRAP - 1);
+      const R z0 = sqrt(R(1) - m0 * m0), z1 = sqrt(R(1) - m1 * m1);
+      const R y0 = z0 * ld_value<R>(law, m0, pv, npar), y1 = z1 * ld_value<R>(law, m1, pv, npar);
+      s += (z1 - z0) * (y1 + y0) / R(2);
     }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     is = R(2.0 * PI) * s;
   }
-  istar[j] = is;
+  if (lane == 0) istar[j] = is;
 }
 
 template <typename R>
@@ -130,9 +144,10 @@ static int ld_tables(int law, const double* ldc, int npv, int npb, int npar, con
                      R* ldp, R* istar, void* stream) {
   if (law < 0 || law >= LD_NLAWS) return RR_ERR_LAW;
   if (npv < 0 || npb < 1 || npar < 0 || npar > MAX_LDPAR || nz < 1) return RR_ERR_ARG;
-  int n = npv * npb;
+  const long long n = (long long)npv * npb;
   if (n == 0) return RR_OK;
-  ld_tables_kernel<R><<<(n + 127) / 128, 128, 0, as_stream(stream)>>>(law, ldc, n, npar, mu, nz, ldp, istar);
+  ld_tables_kernel<R><<<(unsigned)((n + 3) / 4), 128, 0, as_stream(stream)>>>(law, ldc, (int)n, npar, mu, nz, ldp,
+                                                                              istar);
   return check_launch("rr_ld_tables");
 }
 

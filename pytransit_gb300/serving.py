@@ -45,6 +45,13 @@ from . import ldmodels as _ldm
 __all__ = ['Request', 'RRServer', 'GpuExecutor', 'ServerStats', 'ServedFuture']
 
 TILE = 128
+TS_ITEM_TILES = 16     # tiles per work item of a transmission-spectroscopy request (<= 32)
+
+# rr_serve_request (include/pytransit_gb300.h), field by field
+SERVE_REQUEST_DTYPE = np.dtype([('times_ff', 'u8'), ('lcids', 'u8'), ('orb32', 'u8'), ('lc32', 'u8'), ('ldm', 'u8'),
+                                ('flux', 'u8'), ('ldflux', 'i8'), ('npt', 'i4'), ('npv', 'i4'), ('nlc', 'i4'),
+                                ('npb', 'i4'), ('ng', 'i4'), ('kind', 'i4'), ('inv_dg', 'f4'), ('exptime0', 'f4'),
+                                ('dg', 'f8'), ('nsamples0', 'i4'), ('pad', 'i4')])
 
 
 @dataclass
@@ -240,6 +247,17 @@ class _PinnedRing:
         self.live.append((lo, lo + ((n + 255) & ~255), event))
 
 
+def ts_work_items(npv: int, npt: int, tiles: int = TS_ITEM_TILES) -> np.ndarray:
+    """Rows (pv, pv + 1, tile0, tile1) of at most `tiles` tiles each (int32),
+    for a transmission-spectroscopy request: every tile writes all its
+    channel rows, so an item is one pv and a short tile range."""
+    ntiles = max(1, (npt + TILE - 1) // TILE)
+    t0 = np.arange(0, ntiles, tiles)
+    pv = np.repeat(np.arange(npv), t0.size)
+    tt = np.tile(t0, npv)
+    return np.stack([pv, pv + 1, tt, np.minimum(tt + tiles, ntiles)], 1).astype(np.int32)
+
+
 def work_items(npv: int, npt: int, target_tiles: int = 256) -> np.ndarray:
     """Rows (pv0, pv1, tile0, tile1) of about target_tiles pv-tiles each (int32)."""
     ntiles = max(1, (npt + TILE - 1) // TILE)
@@ -413,6 +431,11 @@ class RRServer:
             if req.kind == 'rr':
                 req.state['items'] = work_items(req.npv, req.npt)
                 req.state['icur'] = 0
+            elif req.state.get('persistent'):
+                # a transmission-spectroscopy request whose output fits on the
+                # device: its tiles go through the batched steps as well
+                req.state['items'] = ts_work_items(req.npv, req.npt)
+                req.state['icur'] = 0
             else:
                 self._ts_new.append(req)
             with self._cv:
@@ -423,7 +446,7 @@ class RRServer:
         """Round-robin over active plain requests, up to step_items work items:
         a list of (request, rows of its work items)."""
         batch, n = [], 0
-        rr = [r for r in self._active.values() if r.kind == 'rr' and r.state['icur'] < len(r.state['items'])]
+        rr = [r for r in self._active.values() if 'items' in r.state and r.state['icur'] < len(r.state['items'])]
         while rr and n < self.step_items:
             nxt = []
             share = max(1, (self.step_items - n) // len(rr))
@@ -575,10 +598,7 @@ class GpuExecutor:
         sm = torch.cuda.get_device_properties(self.device).multi_processor_count
         self.nblocks = nblocks or sm * 4
         # request descriptors and item list at fixed device addresses (graph arguments)
-        self.desc_dtype = np.dtype([('times_ff', 'u8'), ('lcids', 'u8'), ('orb32', 'u8'), ('lc32', 'u8'),
-                                    ('ldm', 'u8'), ('flux', 'u8'), ('ldflux', 'i8'), ('npt', 'i4'), ('npv', 'i4'),
-                                    ('nlc', 'i4'), ('npb', 'i4'), ('ng', 'i4'), ('pad0', 'i4'), ('inv_dg', 'f4'),
-                                    ('pad1', 'f4')])
+        self.desc_dtype = SERVE_REQUEST_DTYPE
         self.L.rr_serve_struct_sizes.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
         rs, is_ = C.c_int(), C.c_int()
         self.L.rr_serve_struct_sizes(C.byref(rs), C.byref(is_))
@@ -644,19 +664,24 @@ class GpuExecutor:
         arrays = [(name, h[key]) for name, key in self._INPUTS]
         parts = [(name, a.nbytes) for name, a in arrays]
         n_in = _layout(parts)[1]
-        parts += [('times_ff', 4 * max(int(L.rr_time_split_floats(npt)), 4)), ('ldp', 4 * npv * npb * nz),
-                  ('istar', 4 * npv * npb)]
+        parts += [('times_ff', 4 * max(int(L.rr_time_split_floats(npt)), 4))]
         if req.kind == 'rr':
             nep = h['t0'].shape[1]
             wsb = int(L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng))
-            parts += [('ws', wsb), ('flux', 4 * npv * ldf)]
+            parts += [('ldp', 4 * npv * npb * nz), ('istar', 4 * npv * npb), ('ws', wsb), ('flux', 4 * npv * ldf)]
         else:
+            # the prologue for every pv at admission; the flux through the
+            # batched steps when the whole output fits on the device, else in
+            # pv chunks on a side stream, each chunk copied out as it is done
+            out_bytes = 4 * npv * npb * ldf
+            persistent = self.result == 'device' or out_bytes <= ts_chunk_bytes
             per_pv = max(1, req.nbytes // max(npv, 1))
-            chunk = npv if self.result == 'device' else max(1, min(npv, int(ts_chunk_bytes // per_pv)))
-            wsb = int(L.rr_ts_workspace_bytes(1, chunk, npb, ng))
+            chunk = npv if persistent else max(1, min(npv, int(ts_chunk_bytes // per_pv)))
+            wsb = int(L.rr_ts_workspace_bytes(1, npv, npb, ng))
             parts += [('ws', wsb)]
-            if self.result == 'device':
-                parts += [('flux', 4 * npv * npb * ldf)]
+            if persistent:
+                parts += [('flux', out_bytes)]
+            req.state['persistent'] = persistent
         # a result handed to the caller on the device is a tensor of its own;
         # everything else lives in the request's arena block
         own_flux = self.result == 'device' and req.state.get('keep', True) and 'flux' in dict(parts)
@@ -713,16 +738,33 @@ class GpuExecutor:
                 d['orb32'], d['lc32'], d['ldm'] = orb.value, lc.value, ldm.value
                 d['flux'], d['ldflux'] = P['flux'], ldf
                 d['npt'], d['npv'], d['nlc'], d['npb'], d['ng'] = npt, npv, nlc, npb, ng
-                d['inv_dg'] = np.float32(1.0 / m.dg)
+                d['kind'], d['nsamples0'], d['exptime0'] = 0, 0, 0.0
+                d['dg'], d['inv_dg'] = m.dg, np.float32(1.0 / m.dg)
                 self._dirty.add(slot)
             else:
-                self._lib.check(L.rr_ld_tables_f32(m.ld_law, P['ldc'], npv, npb, npar, tb['mu_ptr'], nz, P['ldp'],
-                                                   P['istar'], sp))
+                # LD profiles, integrals, orbit records and LD means in one launch
+                self._lib.check(L.rr_ts_prepare_split_ld(
+                    m.ld_law, P['ldc'], npar, tb['mu_ptr'], t_ref, t_abs, P['k'], P['t0'], P['p'], P['a'], P['i'],
+                    P['e'], P['w'], npv, npb, float(h['exptimes'][0]), ng, nz, tb['ze_ptr'], P['ws'], wsb, sp),
+                    "rr_ts_prepare_split_ld")
                 g['chunk'] = chunk
-                if self.result == 'device':
+                if req.state['persistent']:
                     n = 4 * npv * npb * ldf
                     g['flux'] = (fl if own_flux else buf[off['flux']:off['flux'] + n].view(torch.float32)
                                  ).view(npv, npb, ldf)
+                    orb, ch, ldm = C.c_void_p(), C.c_void_p(), C.c_void_p()
+                    L.rr_ts_tables(P['ws'], 1, npv, npb, ng, C.byref(orb), C.byref(ch), C.byref(ldm))
+                    slot = self.free_slots.pop()
+                    req.state['slot'] = slot
+                    d = self.descs_h[slot]
+                    d['times_ff'], d['lcids'] = P['times_ff'], 0
+                    d['orb32'], d['lc32'], d['ldm'] = orb.value, ch.value, ldm.value
+                    d['flux'], d['ldflux'] = g['flux'].data_ptr(), ldf
+                    d['npt'], d['npv'], d['nlc'], d['npb'], d['ng'] = npt, npv, 1, npb, ng
+                    d['kind'], d['nsamples0'] = 1, int(h['nsamples'][0])
+                    d['exptime0'] = np.float32(h['exptimes'][0])
+                    d['dg'], d['inv_dg'] = m.dg, np.float32(1.0 / m.dg)
+                    self._dirty.add(slot)
         ready = torch.cuda.Event()
         ready.record(self.setup_stream)
         if stage is self.ring.buf:
@@ -793,9 +835,8 @@ class GpuExecutor:
         def P(name, elems=0, size=8):
             return base[name] + elems * size
 
-        tb = m.tables
         npv, npt, npb = req.npv, req.npt, h['npb']
-        nz, ng = m.ze.size, m.ng
+        ng = m.ng
         ldf = (npt + 3) // 4 * 4
         ns0, ex0 = int(h['nsamples'][0]), float(h['exptimes'][0])
         stream.wait_event(g['ready'])        # set-up kernels of this request
@@ -803,20 +844,10 @@ class GpuExecutor:
             sp = self._lib.stream_ptr(self.device)
 
             def launch(pv0, n, out_ptr):
-                st = L.rr_ts_split(P('times_ff'), g['t_ref'], g['t_abs'], npt, P('k', pv0 * npb), P('t0', pv0),
-                                   P('p', pv0), P('a', pv0), P('i', pv0), P('e', pv0), P('w', pv0), n, npb, ns0,
-                                   ex0, P('ldp', pv0 * npb * nz, 4), P('istar', pv0 * npb, 4), None, m.nk, ng, nz,
-                                   m.dk, float(m.klims[0]), float(m.klims[1]), m.dg, tb['ze_ptr'],
-                                   P('ws'), g['wsb'], out_ptr, ldf, sp)
-                self._lib.check(st, "rr_ts_split")
+                st = L.rr_ts_flux_split_range(P('times_ff'), npt, npv, npb, ns0, ex0, ng, m.dg, P('ws'), pv0,
+                                              pv0 + n, out_ptr, ldf, sp)
+                self._lib.check(st, "rr_ts_flux_split_range")
 
-            if self.result == 'device':
-                launch(0, npv, self._lib.ptr(g['flux']))
-                ev = torch.cuda.Event()
-                ev.record(stream)
-                req.state['host_out'] = g['flux'][:, :, :npt]
-                req.state['ts_done_event'] = ev
-                return
             chunk = g['chunk']
             host = torch.empty((npv, npb, npt), dtype=torch.float32, pin_memory=True)
             req.state['host_out'] = host
@@ -842,18 +873,19 @@ class GpuExecutor:
 
     def start_copy(self, req):
         torch = self.torch
-        if req.kind == 'ts':
+        if req.kind == 'ts' and not req.state.get('persistent'):
             req.state['copy_event'] = req.state['ts_done_event']
             return
         g = req.state['g']
+        res = g['flux'][:, :req.npt] if req.kind == 'rr' else g['flux'][:, :, :req.npt]
         if self.result == 'device':
-            req.state['host_out'] = g['flux'][:, :req.npt]
+            req.state['host_out'] = res
             req.state['copy_event'] = req.state['last_event']
             return
-        host = torch.empty((req.npv, req.npt), dtype=torch.float32, pin_memory=True)
+        host = torch.empty(tuple(res.shape), dtype=torch.float32, pin_memory=True)
         self.copy_stream.wait_event(req.state['last_event'])
         with torch.cuda.stream(self.copy_stream):
-            host.copy_(g['flux'][:, :req.npt], non_blocking=True)
+            host.copy_(res, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(self.copy_stream)
         req.state['host_out'] = host

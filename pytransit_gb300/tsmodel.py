@@ -57,30 +57,49 @@ class TransmissionSpectroscopyModel(RoadRunnerModel):
         ldc3 = np.ascontiguousarray(np.broadcast_to(ldc, (npv, npb, ldc.shape[2])))
         args = self._upload(dict(k=np.ascontiguousarray(k), t0=vecs[0], p=vecs[1], a=vecs[2], i=vecs[3],
                                  e=vecs[4], w=vecs[5], ldc=ldc3 if self.ld_law is not None else None), device)
-        if self.ld_law is not None:
-            ldp = torch.empty((npv, npb, nz), dtype=dt, device=device)
-            istar = torch.empty((npv, npb), dtype=dt, device=device)
-            fn = L.rr_ld_tables_f32 if split else L.rr_ld_tables_f64
-            _lib.check(fn(self.ld_law, P(args['ldc']), npv, npb, ldc3.shape[2], P(tb['mu']), nz, P(ldp), P(istar),
-                          sp), "rr_ld_tables")
-        else:
-            ldp, istar = self._host_ld(ldc3, npv, npb, device, dt)
         ns0 = int(np.atleast_1d(self.nsamples)[0])
         ex0 = float(np.atleast_1d(self.exptimes)[0])
         npt = self.npt
-        ldf = (npt + 3) // 4 * 4 if split else npt
-        W = (tb['W32'] if split else tb['W64']) if self.interpolate else None
+        ldf = (npt + 3) // 4 * 4
         wsb = L.rr_ts_workspace_bytes(int(split), npv, npb, self.ng)
         ws = self._workspace(wsb, device)
         out = torch.empty((npv, npb, ldf), dtype=dt, device=device)
-        common = (P(args['k']), P(args['t0']), P(args['p']), P(args['a']), P(args['i']), P(args['e']), P(args['w']),
-                  npv, npb, ns0, ex0, P(ldp), P(istar), P(W), self.nk, self.ng, nz, self.dk,
-                  float(self.klims[0]), float(self.klims[1]), self.dg, P(tb['ze']), P(ws), ws.numel(), P(out), ldf, sp)
-        if split:
-            st = L.rr_ts_split(P(dd['times_ff']), dd['t_ref'], dd['t_absmax'], npt, *common)
+        orbit = (P(args['k']), P(args['t0']), P(args['p']), P(args['a']), P(args['i']), P(args['e']), P(args['w']))
+        if self.ld_law is not None and not self.interpolate:
+            # a named law with the default 2D table: LD profiles, integrals,
+            # orbit records and LD means in one launch, then the flux
+            if split:
+                st = L.rr_ts_prepare_split_ld(self.ld_law, P(args['ldc']), ldc3.shape[2], P(tb['mu']), dd['t_ref'],
+                                              dd['t_absmax'], *orbit, npv, npb, ex0, self.ng, nz, P(tb['ze']), P(ws),
+                                              ws.numel(), sp)
+                _lib.check(st, "rr_ts_prepare_split_ld")
+                st = L.rr_ts_flux_split(P(dd['times_ff']), npt, npv, npb, ns0, ex0, self.ng, self.dg, P(ws), P(out),
+                                        ldf, sp)
+            else:
+                st = L.rr_ts_prepare_f64_ld(self.ld_law, P(args['ldc']), ldc3.shape[2], P(tb['mu']), *orbit, npv,
+                                            npb, ex0, self.ng, nz, P(tb['ze']), P(ws), ws.numel(), sp)
+                _lib.check(st, "rr_ts_prepare_f64_ld")
+                st = L.rr_ts_flux_f64(P(dd['time']), npt, P(args['t0']), P(args['p']), npv, npb, ns0, ex0, self.ng,
+                                      self.dg, P(ws), P(out), ldf, sp)
+            _lib.check(st, "rr_ts_flux")
         else:
-            st = L.rr_ts_f64(P(dd['time']), npt, *common)
-        _lib.check(st, "rr_ts")
+            if self.ld_law is not None:
+                ldp = torch.empty((npv, npb, nz), dtype=dt, device=device)
+                istar = torch.empty((npv, npb), dtype=dt, device=device)
+                fn = L.rr_ld_tables_f32 if split else L.rr_ld_tables_f64
+                _lib.check(fn(self.ld_law, P(args['ldc']), npv, npb, ldc3.shape[2], P(tb['mu']), nz, P(ldp),
+                              P(istar), sp), "rr_ld_tables")
+            else:
+                ldp, istar = self._host_ld(ldc3, npv, npb, device, dt)
+            W = (tb['W32'] if split else tb['W64']) if self.interpolate else None
+            common = (*orbit, npv, npb, ns0, ex0, P(ldp), P(istar), P(W), self.nk, self.ng, nz, self.dk,
+                      float(self.klims[0]), float(self.klims[1]), self.dg, P(tb['ze']), P(ws), ws.numel(), P(out),
+                      ldf, sp)
+            if split:
+                st = L.rr_ts_split(P(dd['times_ff']), dd['t_ref'], dd['t_absmax'], npt, *common)
+            else:
+                st = L.rr_ts_f64(P(dd['time']), npt, *common)
+            _lib.check(st, "rr_ts")
         out = out[:, :, :npt]
         if copy:
             return out.to(torch.float64).cpu().numpy()
@@ -97,8 +116,8 @@ class TransmissionSpectroscopyModel(RoadRunnerModel):
             else:
                 ldpi = _ldm.evaluate_ld(self.ldmodel, self._ldmu, ldc3)
                 istar = 2 * np.pi * np.trapezoid(self._ldz * ldpi, self._ldz, axis=-1)
-        ldp = np.ascontiguousarray(np.broadcast_to(np.asarray(ldp, np.float64), (npv, npb, self.mu.size)))
-        istar = np.ascontiguousarray(np.broadcast_to(np.asarray(istar, np.float64), (npv, npb)))
+        ldp = np.require(np.broadcast_to(np.asarray(ldp, np.float64), (npv, npb, self.mu.size)), requirements='CW')
+        istar = np.require(np.broadcast_to(np.asarray(istar, np.float64), (npv, npb)), requirements='CW')
         return (torch.as_tensor(ldp).to(device=device, dtype=dt), torch.as_tensor(istar).to(device=device, dtype=dt))
 
     def __call__(self, k, ldc, t0, p, a, i, e=0.0, w=0.0, copy: bool = True):

@@ -154,10 +154,9 @@ def test_serving_struct_layout_matches_binding():
     L.rr_serve_struct_sizes.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
     rs, its = C.c_int(), C.c_int()
     L.rr_serve_struct_sizes(C.byref(rs), C.byref(its))
-    dt = np.dtype([('times_ff', 'u8'), ('lcids', 'u8'), ('orb32', 'u8'), ('lc32', 'u8'), ('ldm', 'u8'),
-                   ('flux', 'u8'), ('ldflux', 'i8'), ('npt', 'i4'), ('npv', 'i4'), ('nlc', 'i4'), ('npb', 'i4'),
-                   ('ng', 'i4'), ('pad0', 'i4'), ('inv_dg', 'f4'), ('pad1', 'f4')])
-    assert rs.value == dt.itemsize and its.value == 24
+    from pytransit_gb300.serving import SERVE_REQUEST_DTYPE as dt
+    assert rs.value == dt.itemsize == 104 and its.value == 24
+    assert [dt.fields[n][1] for n in ('ldflux', 'kind', 'inv_dg', 'dg', 'nsamples0')] == [48, 76, 80, 88, 96]
 
 
 def test_bench_reads_the_profiled_traffic_and_peak():

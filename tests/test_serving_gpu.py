@@ -1,9 +1,12 @@
 """Serving loop on the GPU: every request's flux is the same served alone and
 in a mix of concurrent requests (plain and transmission spectroscopy, three LD
-laws, uneven sizes), and equals the drop-in model's split-precision result.
+laws, uneven sizes), equals the drop-in model's split-precision result, and
+matches the oracle (the reference's algorithm in FP64 on the CPU).
 Tolerance: 1e-6 in flux (the split path's), NaN rows must match."""
 import numpy as np
 import pytest
+
+import oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -49,6 +52,19 @@ def direct(kind, law, data, params):
                       params['i'], params['e'], params['w']).reshape(len(params['p']), -1)
 
 
+def reference(kind, law, data, params):
+    """The oracle's FP64 flux of one request."""
+    if kind == 'ts':
+        ref = oracle.OracleRoadRunner(law, ts=True)
+        ref.set_data(data['time'], nsamples=data['nsamples'][:1], exptimes=data['exptimes'][:1])
+        return ref.evaluate(params['k'], params['ldc'], params['t0'], params['p'], params['a'], params['i'],
+                            params['e'], params['w'])
+    ref = oracle.OracleRoadRunner(law)
+    ref.set_data(**data)
+    return ref.evaluate(params['k'], params['ldc'], params['t0'].reshape(-1, 1), params['p'], params['a'],
+                        params['i'], params['e'], params['w']).reshape(len(params['p']), -1)
+
+
 def close(a, b):
     a, b = np.asarray(a, np.float64), np.asarray(b, np.float64).reshape(a.shape)
     assert np.array_equal(np.isnan(a), np.isnan(b))
@@ -79,4 +95,22 @@ def test_same_alone_and_in_the_mix():
     for r, got, one in zip(reqs, mixed, alone):
         assert close(got, one) <= TOL
         assert close(got, direct(*r)) <= TOL
+        assert close(got, reference(*r)) <= TOL
     assert any(np.nanmin(g) < 0.999 for g in mixed)   # transits are in the data
+
+
+def test_device_results_through_the_persistent_kernel():
+    """With device-resident results every request, transmission spectroscopy
+    included, runs through the batched persistent steps; each result matches
+    the oracle."""
+    from pytransit_gb300.serving import RRServer
+    rng = np.random.default_rng(7)
+    reqs = [make_request(rng, 'ts', 'quadratic', 9, 3000, 1), make_request(rng, 'rr', 'power-2', 40, 5000, 5),
+            make_request(rng, 'ts', 'nonlinear', 4, 7000, 10), make_request(rng, 'ts', 'power-2', 1, 800, 5)]
+    srv = RRServer(hbm_budget=8e9, result='device', step_items=8)
+    futs = [srv.submit(*r) for r in reqs]
+    got = [f.result(timeout=600).cpu().numpy() for f in futs]
+    srv.close()
+    assert srv.stats.completed == len(reqs) and srv.stats.steps > 1
+    for r, g in zip(reqs, got):
+        assert close(g, reference(*r)) <= TOL

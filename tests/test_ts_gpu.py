@@ -104,3 +104,46 @@ def test_ts_short_exposures_vs_oracle(precision, ns, exptime):
     got = m.evaluate(k, ldc, t0, p, a, inc, e, w)
     assert np.sum(want < 1) > 20000
     assert max_err(got, want) <= TOL[precision]
+
+
+def _quad(mu, pv):
+    return 1.0 - pv[0] * (1.0 - mu) - pv[1] * (1.0 - mu) ** 2
+
+
+def _quad_int(pv):
+    return 2 * np.pi / 12 * (-2 * pv[0] - pv[1] + 6)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("law", ["power-2", "nonlinear", "callable", "callable+integral"])
+def test_ts_laws_vs_oracle(precision, law):
+    """The prologue's LD paths: a named law with an analytic disk integral
+    (power-2), one integrated numerically on the device (nonlinear), and a
+    user callable evaluated on the host with or without its integral (the
+    profiles and integrals then come from the host, as in the serving loop)."""
+    from pytransit_gb300 import TransmissionSpectroscopyModel
+    rng = np.random.default_rng(11)
+    T = 2459000.0
+    time = T + np.linspace(-0.2, 0.2, 1500)
+    npv, npb = 5, 150
+    k = rng.uniform(0.09, 0.11, (npv, npb))
+    if law == "power-2":
+        ldc = np.stack([rng.uniform(.3, .9, (npv, npb)), rng.uniform(.3, .8, (npv, npb))], -1)
+    elif law == "nonlinear":
+        ldc = np.tile([0.5, -0.2, 0.6, -0.25], (npv, npb, 1)) * rng.uniform(0.8, 1.2, (npv, npb, 1))
+    else:
+        ldc = np.stack([rng.uniform(0.2, 0.5, (npv, npb)), rng.uniform(0.1, 0.3, (npv, npb))], -1)
+    ldm = {"callable": _quad, "callable+integral": (_quad, _quad_int)}.get(law, law)
+    t0 = T + rng.normal(0, 1e-3, npv)
+    p = rng.uniform(1, 5, npv)
+    a = rng.uniform(4, 12, npv)
+    inc = np.arccos(rng.uniform(0, 0.8, npv) / a)
+    e, w = rng.uniform(0, 0.2, npv), rng.uniform(0, 2 * np.pi, npv)
+    ref = oracle.OracleRoadRunner(ldm, ts=True)
+    ref.set_data(time, nsamples=[3], exptimes=[0.01])
+    want = ref.evaluate(k, ldc, t0, p, a, inc, e, w)
+    m = TransmissionSpectroscopyModel(ldm, precision=precision)
+    m.set_data(time, nsamples=[3], exptimes=[0.01])
+    got = m.evaluate(k, ldc, t0, p, a, inc, e, w)
+    assert np.sum(want < 1) > 5000
+    assert max_err(got, want) <= TOL[precision]
