@@ -303,7 +303,7 @@ def bench_c2(torch, device, steps=5, n_oracle=256):
             "timed": "RoadRunnerModel.evaluate(copy=False), CUDA events, parameters uploaded each call"}
 
 
-def bench_ts(torch, device, steps=5, npv=64, npb=200, npt=19700):
+def bench_ts(torch, device, steps=20, npv=64, npb=200, npt=19700):
     """Transmission spectroscopy: 64 pv x 200 channels x 19,700 times (2-min
     cadence), quadratic LD, k ~ U(0.09, 0.11), one sample per point."""
     from pytransit_gb300 import TSModel
@@ -391,7 +391,7 @@ def bench_ts(torch, device, steps=5, npv=64, npb=200, npt=19700):
                 "timed": "rr_ts_prepare_split_ld + rr_ts_flux_split through the C ABI, inputs in HBM, CUDA events"}}
 
 
-def bench_c3(torch, device, steps=3):
+def bench_c3(torch, device, steps=10):
     """Log-likelihood + adjoint gradient, 4096 pv x 5000 times, 5 supersamples."""
     from pytransit_gb300 import RoadRunnerModel
     from pytransit_gb300.lnlike import lnlikelihood
@@ -421,7 +421,7 @@ def bench_c3(torch, device, steps=3):
         lnlikelihood(*args, grad=True, copy=False)
         torch.cuda.synchronize(device)
         t = time.perf_counter()
-        n = steps if prec == "split" else 1
+        n = steps if prec == "split" else 2
         for _ in range(n):
             lnl, g = lnlikelihood(*args, grad=True, copy=False)
         torch.cuda.synchronize(device)
@@ -429,12 +429,73 @@ def bench_c3(torch, device, steps=3):
     g32, g64 = out["split"][2], out["fp64"][2]
     col_rel = float((np.abs(g32 - g64) / np.abs(g64).max(axis=0, keepdims=True)).max())
     lnl_rel = float(np.abs(out["split"][1] - out["fp64"][1]).max() / np.abs(out["fp64"][1]).max())
+    # central finite differences of the FP64 log-likelihood at the full size
+    # (h = 1e-6 relative, with floors), element by element: |g - fd| against
+    # 1e-4 |fd| plus the differences' own rounding floor (16 ulps of |lnL|
+    # over the step), plus 1e-6 of the column's largest |fd| for the split path
+    m64 = RoadRunnerModel('quadratic', precision='fp64', device=device)
+    m64.set_data(**data)
+    floors = dict(k=1e-3, t0=1e-2, p=1.0, a=1.0, i=1.0, e=1e-2, w=1e-1, ldc=1e-2)
+    spec = [('k', (slice(None), 0)), ('t0', (slice(None), 0)), ('p', ()), ('a', ()), ('i', ()), ('e', ()),
+            ('w', ()), ('ldc', (slice(None), 0, 0)), ('ldc', (slice(None), 0, 1))]
+
+    def lnl64(q):
+        return lnlikelihood(m64, obs, sigma, q["k"], q["ldc"], q["t0"], q["p"], q["a"], q["i"], q["e"], q["w"])
+
+    base = {n: np.array(v, dtype=np.float64, copy=True) for n, v in prm.items()}
+    lnl0 = np.abs(lnl64(base))
+
+    def central(scale):
+        fd_, fl_ = [], []
+        for name, idx in spec:
+            x = base[name][idx] if idx else base[name]
+            h = scale * 1e-6 * np.maximum(np.abs(x), floors[name])
+            up = {n: v.copy() for n, v in base.items()}
+            dn = {n: v.copy() for n, v in base.items()}
+            if idx:
+                up[name][idx], dn[name][idx] = x + h, x - h
+                step = up[name][idx] - dn[name][idx]
+            else:
+                up[name], dn[name] = x + h, x - h
+                step = up[name] - dn[name]
+            fd_.append((lnl64(up) - lnl64(dn)) / step)
+            fl_.append(16 * np.finfo(np.float64).eps * lnl0 / step)
+        return np.stack(fd_, -1), np.stack(fl_, -1)
+
+    # the FD's uncertainty: its rounding, and its truncation (large where a step
+    # crosses a kink of the piecewise-linear LD tables) as |FD(h) - FD(h/2)|
+    fd_h, _ = central(0.01)
+    fd, fl = central(0.005)
+    fl = fl + np.abs(fd_h - fd)
+    fd_check = {}
+    # e = 0 (clipped) leaves no room for the step below: those elements have no central difference
+    fin = np.isfinite(fd) & np.isfinite(fl)
+    colmax = np.nanmax(np.where(fin, np.abs(fd), np.nan), axis=0, keepdims=True)
+    for prec, g in (("fp64", g64), ("split", g32)):
+        err = (np.abs(g - fd) / (1e-4 * np.abs(fd) + fl))[fin]
+        big = fin & (np.abs(fd) > 100 * fl)
+        fd_check[prec] = {"max_err_over_bound": float(err.max()), "elements_within_bound": float((err <= 1).mean()),
+                          "max_rel_err_where_fd_above_100_floors": float((np.abs(g - fd) / np.abs(fd))[big].max()),
+                          "max_abs_err_over_column_scale": float((np.abs(g - fd) / colmax)[fin].max())}
+    fd_check["elements_without_central_difference"] = int((~fin).sum())
+    # a repeated call gives the same bits (sums in a fixed order)
+    msplit = RoadRunnerModel('quadratic', precision='split', device=device)
+    msplit.set_data(**data)
+    a1 = lnlikelihood(msplit, obs, sigma, prm["k"], prm["ldc"], prm["t0"], prm["p"], prm["a"], prm["i"], prm["e"],
+                      prm["w"], grad=True)
+    a2 = lnlikelihood(msplit, obs, sigma, prm["k"], prm["ldc"], prm["t0"], prm["p"], prm["a"], prm["i"], prm["e"],
+                      prm["w"], grad=True)
+    reproducible = bool(np.array_equal(a1[0], a2[0]) and np.array_equal(a1[1], a2[1]))
     return {"workload": f"{npv} pv x {npt} times, 5 supersamples, quadratic LD, Gaussian lnL sigma=5e-4, "
                         "gradient wrt (k, t0, p, a, i, e, w, u1, u2)",
             "split_ms": out["split"][0] * 1e3, "fp64_ms": out["fp64"][0] * 1e3,
             "split_points_per_s": npv * npt / out["split"][0], "fp64_points_per_s": npv * npt / out["fp64"][0],
             "split_over_fp64": out["fp64"][0] / out["split"][0],
             "grad_max_rel_err_split_vs_fp64": col_rel, "lnl_max_rel_err_split_vs_fp64": lnl_rel,
+            "grad_vs_fd": dict(fd_check, what="per element: |g - fd| / (1e-4 |fd| + floor) <= 1 is within the "
+                                              "1e-4 relative target; FD of the FP64 lnL, h = 5e-9 relative; floor = "
+                                              "16 ulps of |lnL| / step + |FD(2h) - FD(h)|"),
+            "bit_reproducible": reproducible,
             "timed": "lnlikelihood(grad=True) end to end (LD tables, prologue, fused lnL + adjoint), wall clock"}
 
 

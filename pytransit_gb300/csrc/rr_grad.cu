@@ -20,7 +20,6 @@
 
 namespace rr {
 
-constexpr int GRAD_THREADS = 256;
 constexpr int MAX_GRAD_PAR = 4;    // LD coefficients per passband in the adjoint
 constexpr int MAX_NGRAD = 64;      // nkc + nep + 5 + npb * npar
 constexpr int GLC_SMEM = 64;       // light-curve records staged in shared memory (split)
@@ -146,16 +145,23 @@ grad_ld_kernel(int law, const double* __restrict__ ldc, int npb, int npar, const
 
 // ---------------------------------------------------------------------------
 // Observations: dobs[i] = o_i - 1 and isig2[i] = 1/sigma_lc^2 in R, and the
-// pv-independent constant of lnL (one block, FP64).
+// pv-independent constant of lnL in per-block parts (FP64, fixed order), one
+// block per OBS_CHUNK points.
 // ---------------------------------------------------------------------------
+constexpr int OBS_THREADS = 128;
+constexpr int OBS_CHUNK = OBS_THREADS * 4;
+
 template <typename R>
-__global__ void obs_kernel(const double* __restrict__ obs, const double* __restrict__ sigma,
-                           const int32_t* __restrict__ lcids, int npt, R* __restrict__ dobs,
-                           R* __restrict__ isig2, double* __restrict__ cconst) {
-  __shared__ double red[32];
+__global__ void __launch_bounds__(OBS_THREADS) obs_kernel(const double* __restrict__ obs,
+                                                          const double* __restrict__ sigma,
+                                                          const int32_t* __restrict__ lcids, int npt,
+                                                          R* __restrict__ dobs, R* __restrict__ isig2,
+                                                          double* __restrict__ cpart) {
+  __shared__ double red[OBS_THREADS / 32];
   double acc = 0.0;
   const double hl2pi = 0.5 * log(2.0 * PI);
-  for (int i = threadIdx.x; i < npt; i += blockDim.x) {
+  const int i0 = blockIdx.x * OBS_CHUNK, i1 = min(npt, i0 + OBS_CHUNK);
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     const double s = sigma[lcids[i]];
     const double d = obs[i] - 1.0;
     dobs[i] = (R)d;
@@ -166,19 +172,20 @@ __global__ void obs_kernel(const double* __restrict__ obs, const double* __restr
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
-    *cconst = s;
+    double sm = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) sm += red[i];
+    cpart[blockIdx.x] = sm;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Main kernel: one thread per (pv, point).  For in-box points: per sample the
-// sky position and its derivatives (Horner on c and on dc), z, the area and
-// its partials, the interpolated mean intensity and its partials; per point
-// D = sum_s I A / (ns istar) and dD/dtheta; lnL gets -(do + D/2) D / sigma^2,
-// the gradient -(r / sigma^2) dD/dtheta with r = do + D.  Block sums go to
-// partials[pv][block][1 + ngrad] (FP64).
+// Main kernel: blocks over (chunk of points, pv), each thread a few points.
+// For in-box points: per sample the sky position and its derivatives (Horner
+// on c and on dc), z, the area and its partials, the interpolated mean
+// intensity and its partials; per point D = sum_s I A / (ns istar); lnL gets
+// -(do + D/2) D / sigma^2, the gradient -(r / sigma^2) dD/dtheta with
+// r = do + D.  Block sums go to partials[pv][block][1 + ngrad] (FP64), summed
+// per pv in block order by lnlike_reduce_kernel: no step depends on timing.
 // ---------------------------------------------------------------------------
 template <typename R>
 struct GradArgs {
@@ -211,95 +218,105 @@ __device__ __forceinline__ int grad_col(int slot, int nkc, int nep, int npar, in
   }
 }
 
-template <typename R, bool SPLIT>
-__global__ void __launch_bounds__(GRAD_THREADS) lnlike_kernel(GradArgs<R> A) {
-  __shared__ double red[1 + MAX_NGRAD];
-  __shared__ __align__(16) float lcs[SPLIT ? GLC_SMEM * LC32 : 1];
-  __shared__ R orbc[10];
-  __shared__ R dcs[50];
-  const unsigned FULL = 0xffffffffu;
-  const int pv = blockIdx.y;
-  const int pt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  for (int i = threadIdx.x; i <= A.ngrad; i += blockDim.x) red[i] = 0.0;
-  if (threadIdx.x < 10)
-    orbc[threadIdx.x] = SPLIT ? (R)A.orb32[(size_t)pv * ORB32 + threadIdx.x] : (R)A.orb64[(size_t)pv * ORB64 + threadIdx.x];
-  if (threadIdx.x < 50) dcs[threadIdx.x] = A.dc[(size_t)pv * 50 + threadIdx.x];
-  const bool lc_smem = SPLIT && A.nlc <= GLC_SMEM;
-  if (lc_smem)
-    for (int i = threadIdx.x; i < A.nlc * LC32; i += blockDim.x) lcs[i] = A.lc32[(size_t)pv * A.nlc * LC32 + i];
-  __syncthreads();
-  const bool valid = SPLIT ? (__float_as_int(A.orb32[(size_t)pv * ORB32 + 14]) & FLAG_VALID)
-                           : (A.orb64[(size_t)pv * ORB64 + 12] != 0.0);
+// Launch shape of the likelihood kernel: blocks of LNL_THREADS threads over
+// LNL_CHUNK consecutive points of one pv, LNL_PPT points per thread.
+constexpr int LNL_THREADS = 128;
+constexpr int LNL_PPT = 8;
+constexpr int LNL_CHUNK = LNL_THREADS * LNL_PPT;
+constexpr int LNL_NW = LNL_THREADS / 32;
 
-  R slot[GS_NSLOT];
-  for (int s = 0; s < GS_NSLOT; ++s) slot[s] = R(0);
-  int lc = 0, pb = 0, ep = 0;
-  bool inbox = false;
-  R tc = R(0), nep_count = R(0);
-  if (valid && pt < A.npt) {
-    lc = A.lcids[pt];
-    pb = A.pbids[lc];
-    ep = A.epids[lc];
-    if (SPLIT) {
-      const float* LCR = lc_smem ? lcs + lc * LC32 : A.lc32 + ((size_t)pv * A.nlc + lc) * LC32;
-      const float* o = A.orb32 + (size_t)pv * ORB32;
-      const float p_hi = o[10], p_lo = o[11], inv_p = o[12];
-      const float2 tt = A.times_ff[pt];
-      const float d0h = LCR[LC_D0H], d0l = LCR[LC_D0L];
-      float n = floorf(fmaf(tt.x - d0h, inv_p, 0.5f));
-      float s1, e1, q1, e2, s2, e3;
-      two_sum(tt.x, -d0h, s1, e1);
+// Adds one point's terms to the slot accumulators acc (the lnL term and, with
+// GRAD, the gradient terms of GS_KK ... GS_C0 + npar - 1); nothing for a point
+// out of the box.  Two passes over the samples: the first gives the point's
+// deficit D and with it the residual weight -(r / sigma^2) / (ns istar); the
+// second recomputes each sample and adds its derivative terms, already
+// scaled by that weight, straight into acc (no per-point sums are kept).
+template <typename R, bool SPLIT, bool GRAD>
+__device__ __forceinline__ void lnlike_point(const GradArgs<R>& A, int pv, int pt, int lc, const float* lcs,
+                                             bool lc_smem, const R* orbc, const R* dcs, R* acc) {
+  const int pb = A.pbids[lc], ep = A.epids[lc];
+  bool inbox;
+  R tc, nep_count;
+  if (SPLIT) {
+    const float* LCR = lc_smem ? lcs + lc * LC32 : A.lc32 + ((size_t)pv * A.nlc + lc) * LC32;
+    const float* o = A.orb32 + (size_t)pv * ORB32;
+    const float p_hi = o[10], p_lo = o[11], inv_p = o[12];
+    const float2 tt = A.times_ff[pt];
+    const float d0h = LCR[LC_D0H], d0l = LCR[LC_D0L];
+    float n = floorf(fmaf(tt.x - d0h, inv_p, 0.5f));
+    float s1, e1, q1, e2, s2, e3;
+    two_sum(tt.x, -d0h, s1, e1);
+    two_prod(n, p_hi, q1, e2);
+    two_sum(s1, -q1, s2, e3);
+    float t = s2 + (((e1 + e3) - e2) + (tt.y - d0l) - n * p_lo);
+    if (t >= 0.5f * p_hi || t < -0.5f * p_hi) {
+      n += (t >= 0.5f * p_hi) ? 1.0f : -1.0f;
       two_prod(n, p_hi, q1, e2);
       two_sum(s1, -q1, s2, e3);
-      float t = s2 + (((e1 + e3) - e2) + (tt.y - d0l) - n * p_lo);
-      if (t >= 0.5f * p_hi || t < -0.5f * p_hi) {
-        n += (t >= 0.5f * p_hi) ? 1.0f : -1.0f;
-        two_prod(n, p_hi, q1, e2);
-        two_sum(s1, -q1, s2, e3);
-        t = s2 + (((e1 + e3) - e2) + (tt.y - d0l) - n * p_lo);
-      }
-      inbox = (LCR[LC_LO] <= t && t <= LCR[LC_HI]);
-      tc = (R)t;
-      nep_count = (R)n;
-    } else {
-      const double t = A.times[pt];
-      const double t0 = A.t0[(size_t)pv * A.ldt0 + ep];
-      const double p = A.p[pv];
-      const double epoch = floor(__ddiv_rn(__dadd_rn(__dsub_rn(t, t0), __dmul_rn(0.5, p)), p));
-      const double tcd = __dsub_rn(t, __dadd_rn(t0, __dmul_rn(epoch, p)));
-      const double pad = __dadd_rn(0.003, A.exptimes[lc]);
-      const double* o = A.orb64 + (size_t)pv * ORB64;
-      inbox = (__dsub_rn(o[10], pad) <= tcd && tcd <= __dadd_rn(o[11], pad));
-      tc = (R)tcd;
-      nep_count = (R)epoch;
+      t = s2 + (((e1 + e3) - e2) + (tt.y - d0l) - n * p_lo);
     }
+    inbox = (LCR[LC_LO] <= t && t <= LCR[LC_HI]);
+    tc = (R)t;
+    nep_count = (R)n;
+  } else {
+    const double t = A.times[pt];
+    const double t0 = A.t0[(size_t)pv * A.ldt0 + ep];
+    const double p = A.p[pv];
+    const double epoch = floor(__ddiv_rn(__dadd_rn(__dsub_rn(t, t0), __dmul_rn(0.5, p)), p));
+    const double tcd = __dsub_rn(t, __dadd_rn(t0, __dmul_rn(epoch, p)));
+    const double pad = __dadd_rn(0.003, A.exptimes[lc]);
+    const double* o = A.orb64 + (size_t)pv * ORB64;
+    inbox = (__dsub_rn(o[10], pad) <= tcd && tcd <= __dadd_rn(o[11], pad));
+    tc = (R)tcd;
+    nep_count = (R)epoch;
   }
-  if (inbox) {
-    R kk, inv_is, ex, inv_ns;
-    int ns;
-    if (SPLIT) {
-      const float* LCR = lc_smem ? lcs + lc * LC32 : A.lc32 + ((size_t)pv * A.nlc + lc) * LC32;
-      kk = (R)LCR[LC_K];
-      inv_is = (R)LCR[LC_INVIS];
-      ex = (R)LCR[LC_EXPT];
-      inv_ns = (R)LCR[LC_INVNS];
-      ns = __float_as_int(LCR[LC_NS]);
-    } else {
-      kk = (R)A.k[(size_t)pv * A.nkc + (A.nkc == A.npb ? pb : 0)];
-      inv_is = R(1) / (R)A.istar64[(size_t)pv * A.npb + pb];
-      ex = (R)A.exptimes[lc];
-      ns = A.nsamples[lc];
-      inv_ns = R(1) / (R)ns;
+  if (!inbox) return;
+  R kk, inv_is, ex, inv_ns;
+  int ns;
+  if (SPLIT) {
+    const float* LCR = lc_smem ? lcs + lc * LC32 : A.lc32 + ((size_t)pv * A.nlc + lc) * LC32;
+    kk = (R)LCR[LC_K];
+    inv_is = (R)LCR[LC_INVIS];
+    ex = (R)LCR[LC_EXPT];
+    inv_ns = (R)LCR[LC_INVNS];
+    ns = __float_as_int(LCR[LC_NS]);
+  } else {
+    kk = (R)A.k[(size_t)pv * A.nkc + (A.nkc == A.npb ? pb : 0)];
+    inv_is = R(1) / (R)A.istar64[(size_t)pv * A.npb + pb];
+    ex = (R)A.exptimes[lc];
+    ns = A.nsamples[lc];
+    inv_ns = R(1) / (R)ns;
+  }
+  const R inv1pk = R(1) / (R(1) + kk);
+  const R inv_dg = R(1) / (R)A.dg;
+  const size_t ppb = (size_t)pv * A.npb + pb;
+  const R* L = A.ldm + ppb * A.ng;
+  // pass 1: the deficit D = sum_s I A / (ns istar)
+  R SQ = R(0);
+  for (int s = 0; s < ns; ++s) {
+    const R t = tc + ex * ((R(s) + R(0.5)) * inv_ns - R(0.5));
+    R x = orbc[4], y = orbc[9];
+    for (int m = 3; m >= 0; --m) {
+      x = x * t + orbc[m];
+      y = y * t + orbc[5 + m];
     }
-    const R inv1pk = R(1) / (R(1) + kk);
-    const R inv_dg = R(1) / (R)A.dg;
-    const size_t ppb = (size_t)pv * A.npb + pb;
-    const R* L = A.ldm + ppb * A.ng;
+    const R z = sqrt(x * x + y * y);
+    if (!(z < R(1) + kk)) continue;  // A = 0 and I A = 0 beyond first contact
+    const R gg = z * inv1pk * inv_dg;
+    const int i = min(max((int)gg, 0), A.ng - 2);
+    const R fr = gg - (R)i;
+    const R l0 = L[i], l1 = L[i + 1];
+    R kap;
+    SQ += (l0 + fr * (l1 - l0)) * ccia_star<R>(kk, z, kap);
+  }
+  const R sc = inv_is * inv_ns;
+  const R D = SQ * sc;
+  const R do_ = A.dobs[pt], w = A.isig2[pt];
+  acc[GS_LNL] += -(do_ + R(0.5) * D) * D * w;
+  if constexpr (GRAD) {
+    const R gsc = -(do_ + D) * w * sc;    // -(r / sigma^2) / (ns istar)
     const R* T = A.tab + ppb * (size_t)(1 + A.npar) * A.ng;
-    R SQ = R(0), SKK = R(0), SKW = R(0);
-    R SZ[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};   // t0, p, a, i, e, w
-    R SC[MAX_GRAD_PAR] = {};
+    // pass 2: the derivative terms of every sample, times gsc
     for (int s = 0; s < ns; ++s) {
       const R t = tc + ex * ((R(s) + R(0.5)) * inv_ns - R(0.5));
       R x = orbc[4], y = orbc[9], xd = R(4) * orbc[4], yd = R(4) * orbc[9];
@@ -312,30 +329,32 @@ __global__ void __launch_bounds__(GRAD_THREADS) lnlike_kernel(GradArgs<R> A) {
         }
       }
       const R z = sqrt(x * x + y * y);
-      if (!(z < R(1) + kk)) continue;  // A = 0 and I A = 0 beyond first contact
-      const R iz = R(1) / z;
-      const R dzdt = (x * xd + y * yd) * iz;
+      if (!(z < R(1) + kk)) continue;
       const R g = z * inv1pk;
       const R gg = g * inv_dg;
-      int i = (int)gg;
-      i = min(max(i, 0), A.ng - 2);
+      const int i = min(max((int)gg, 0), A.ng - 2);
       const R fr = gg - (R)i;
       const R l0 = L[i], l1 = L[i + 1];
       const R ip = l0 + fr * (l1 - l0);
-      const R dIdg = (l1 - l0) * inv_dg;
       R dadk, dadz;
       const R ar = ccia_star_grad<R>(kk, z, dadk, dadz);
-      SQ += ip * ar;
-      if (!A.grad) continue;
-      const R dQdz = dIdg * inv1pk * ar + ip * dadz;
-      SKK += -dIdg * g * inv1pk * ar + ip * dadk;
-      SKW += (T[i] + fr * (T[i + 1] - T[i])) * ar;
-      for (int j = 0; j < A.npar; ++j) {
-        const R* Tj = T + (size_t)(1 + j) * A.ng;
-        SC[j] += (Tj[i] + fr * (Tj[i + 1] - Tj[i])) * ar;
+      const R gar = gsc * ar;
+      const R iz = R(1) / z;
+      const R dzdt = (x * xd + y * yd) * iz;
+      const R dIdg = (l1 - l0) * inv_dg;
+      const R gdz = gsc * (dIdg * inv1pk * ar + ip * dadz);   // gsc dQ/dz
+      acc[GS_KK] += gsc * (-dIdg * g * inv1pk * ar + ip * dadk);
+      acc[GS_KW] += (T[i] + fr * (T[i + 1] - T[i])) * gar;
+#pragma unroll
+      for (int j = 0; j < MAX_GRAD_PAR; ++j) {
+        if (j < A.npar) {
+          const R* Tj = T + (size_t)(1 + j) * A.ng;
+          acc[GS_C0 + j] += (Tj[i] + fr * (Tj[i + 1] - Tj[i])) * gar;
+        }
       }
       // dz/dtheta: orbit coefficients (p, a, i, e, w) and the time shift of t0, p
-      SZ[0] += dQdz * (-dzdt);
+      acc[GS_T0] += gdz * (-dzdt);
+#pragma unroll
       for (int jj = 0; jj < 5; ++jj) {
         const R* d = dcs + jj * 10;
         R dx = d[4], dy = d[9];
@@ -345,60 +364,119 @@ __global__ void __launch_bounds__(GRAD_THREADS) lnlike_kernel(GradArgs<R> A) {
         }
         R dz = (x * dx + y * dy) * iz;
         if (jj == 0) dz += dzdt * (-nep_count);
-        SZ[1 + jj] += dQdz * dz;
+        acc[GS_P + jj] += gdz * dz;
       }
     }
-    const R sc = inv_is * inv_ns;
-    const R D = SQ * sc;
-    const R do_ = A.dobs[pt], w = A.isig2[pt];
-    slot[GS_LNL] = -(do_ + R(0.5) * D) * D * w;
-    if (A.grad) {
-      const R gsc = -(do_ + D) * w * sc;    // -(r / sigma^2) / (ns istar)
-      slot[GS_KK] = gsc * SKK;
-      slot[GS_KW] = gsc * SKW;
-      slot[GS_T0] = gsc * SZ[0];
-      for (int jj = 0; jj < 5; ++jj) slot[GS_P + jj] = gsc * SZ[1 + jj];
-      const R* dI = A.dis + ppb * A.npar;
-      for (int j = 0; j < A.npar; ++j)
-        slot[GS_C0 + j] = gsc * SC[j] - (-(do_ + D) * w) * D * inv_is * dI[j];
-    }
+    // the disk integral's dependence on the LD coefficients
+    const R* dI = A.dis + ppb * A.npar;
+#pragma unroll
+    for (int j = 0; j < MAX_GRAD_PAR; ++j)
+      if (j < A.npar) acc[GS_C0 + j] += (do_ + D) * w * D * inv_is * dI[j];
   }
-  // block reduction: warp sums where every lane of the warp shares a destination,
-  // shared-memory atomics otherwise
-  const bool uni = __all_sync(FULL, lc == __shfl_sync(FULL, lc, 0));
-  const int nsl = A.grad ? GS_C0 + A.npar : 1;
-  for (int s = 0; s < nsl; ++s) {
-    const int col = (s == GS_LNL) ? -1 : grad_col(s, A.nkc, A.nep, A.npar, pb, ep, s - GS_C0);
-    if (!uni) {
-      if (slot[s] != R(0)) atomicAdd(&red[col + 1], (double)slot[s]);
-      continue;
-    }
-    if constexpr (sizeof(R) == 4) {
-      // FP32 (hi, lo) pairs summed with error-free two-sums: the warp sum is
-      // as accurate as an FP64 one without the FP64 pipe (1/64 rate)
-      float hi = slot[s], lo = 0.0f;
-      for (int o = 16; o > 0; o >>= 1) {
-        const float h2 = __shfl_down_sync(FULL, hi, o), l2 = __shfl_down_sync(FULL, lo, o);
-        float sh, se;
-        two_sum(hi, h2, sh, se);
-        lo = lo + l2 + se;
-        hi = sh;
+}
+
+// Adds the accumulators of the lanes in `pending` to the warp's row of
+// shared FP64 sums, one group of lanes sharing a light curve at a time
+// (lowest lane first), each slot by the same shuffle tree; then clears them.
+// Every step is in a fixed order, so the sums are reproducible bit for bit.
+template <typename R, int NS>
+__device__ __forceinline__ void lnlike_flush(const GradArgs<R>& A, R* acc, int key, bool pending, double* row) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int nsl = NS > 1 ? GS_C0 + A.npar : 1;
+  unsigned pend = __ballot_sync(FULL, pending);
+  while (pend) {
+    const int leader = __ffs(pend) - 1;
+    const int kl = __shfl_sync(FULL, key, leader);
+    const unsigned mem = __ballot_sync(FULL, pending && key == kl) & pend;
+    const bool in = (mem >> lane) & 1u;
+    const int pb = A.pbids[kl], ep = A.epids[kl];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      if (s >= nsl) break;
+      const int col = (s == GS_LNL) ? -1 : grad_col(s, A.nkc, A.nep, A.npar, pb, ep, s - GS_C0);
+      double tot;
+      if constexpr (sizeof(R) == 4) {
+        // FP32 (hi, lo) pairs summed with error-free two-sums: as accurate as
+        // an FP64 tree without the FP64 pipe (1/64 rate)
+        float hi = in ? acc[s] : 0.0f, lo = 0.0f;
+        for (int o = 16; o > 0; o >>= 1) {
+          const float h2 = __shfl_down_sync(FULL, hi, o), l2 = __shfl_down_sync(FULL, lo, o);
+          float sh, se;
+          two_sum(hi, h2, sh, se);
+          lo = lo + l2 + se;
+          hi = sh;
+        }
+        tot = (double)hi + (double)lo;
+      } else {
+        double vv = in ? (double)acc[s] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) vv += __shfl_down_sync(FULL, vv, o);
+        tot = vv;
       }
-      if (lane == 0 && (hi != 0.0f || lo != 0.0f)) atomicAdd(&red[col + 1], (double)hi + (double)lo);
-    } else {
-      double v = (double)slot[s];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
-      if (lane == 0 && v != 0.0) atomicAdd(&red[col + 1], v);
+      if (lane == 0) row[col + 1] += tot;
     }
+    if (in) {
+#pragma unroll
+      for (int s = 0; s < NS; ++s) acc[s] = R(0);
+    }
+    pend &= ~mem;
   }
+}
+
+// One block: LNL_CHUNK consecutive points of pv.  Each thread sums its points'
+// terms in registers while they share a light curve (the gradient columns
+// depend on its passband and epoch), flushing to its warp's row of shared
+// sums when the light curve changes and at the end; the block writes the sum
+// of the warps' rows, in warp order, to its slot of partials.
+template <typename R, bool SPLIT, bool GRAD>
+__global__ void __launch_bounds__(LNL_THREADS, sizeof(R) == 4 ? 4 : 2) lnlike_kernel(GradArgs<R> A) {
+  constexpr int NS = GRAD ? GS_NSLOT : 1;
+  __shared__ double wred[LNL_NW][1 + MAX_NGRAD];
+  __shared__ __align__(16) float lcs[SPLIT ? GLC_SMEM * LC32 : 1];
+  __shared__ R orbc[10];
+  __shared__ R dcs[50];
+  const int pv = blockIdx.y;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < LNL_NW * (1 + MAX_NGRAD); i += blockDim.x) (&wred[0][0])[i] = 0.0;
+  if (tid < 10)
+    orbc[tid] = SPLIT ? (R)A.orb32[(size_t)pv * ORB32 + tid] : (R)A.orb64[(size_t)pv * ORB64 + tid];
+  if (GRAD && tid < 50) dcs[tid] = A.dc[(size_t)pv * 50 + tid];
+  const bool lc_smem = SPLIT && A.nlc <= GLC_SMEM;
+  if (lc_smem)
+    for (int i = tid; i < A.nlc * LC32; i += blockDim.x) lcs[i] = A.lc32[(size_t)pv * A.nlc * LC32 + i];
+  __syncthreads();
+  const bool valid = SPLIT ? (__float_as_int(A.orb32[(size_t)pv * ORB32 + 14]) & FLAG_VALID)
+                           : (A.orb64[(size_t)pv * ORB64 + 12] != 0.0);
+  R acc[NS];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) acc[s] = R(0);
+  int key = -1;
+  for (int j = 0; j < LNL_PPT; ++j) {
+    const int pt = blockIdx.x * LNL_CHUNK + j * LNL_THREADS + tid;
+    const int lc = (valid && pt < A.npt) ? A.lcids[pt] : -1;
+    const bool flush = key >= 0 && lc >= 0 && lc != key;
+    if (__any_sync(0xffffffffu, flush)) {
+      lnlike_flush<R, NS>(A, acc, key, flush, wred[warp]);
+      if (flush) key = -1;
+    }
+    if (lc < 0) continue;
+    lnlike_point<R, SPLIT, GRAD>(A, pv, pt, lc, lcs, lc_smem, orbc, dcs, acc);
+    key = lc;
+  }
+  lnlike_flush<R, NS>(A, acc, key, key >= 0, wred[warp]);
   __syncthreads();
   double* out = A.partials + ((size_t)pv * gridDim.x + blockIdx.x) * (1 + A.ngrad);
-  for (int i = threadIdx.x; i <= A.ngrad; i += blockDim.x) out[i] = red[i];
+  for (int i = tid; i <= A.ngrad; i += blockDim.x) {
+    double sm = 0.0;
+#pragma unroll
+    for (int w = 0; w < LNL_NW; ++w) sm += wred[w][i];
+    out[i] = sm;
+  }
 }
 
 // Sum the block partials of each pv in a fixed order; invalid pv -> NaN.
 __global__ void lnlike_reduce_kernel(const double* __restrict__ partials, int nblk, int ngrad, int npv,
-                                     const double* __restrict__ cconst, const double* __restrict__ orb64,
+                                     const double* __restrict__ cpart, int ncpart, const double* __restrict__ orb64,
                                      const float* __restrict__ orb32, double* __restrict__ lnl,
                                      double* __restrict__ grad) {
   const int pv = blockIdx.x;
@@ -408,7 +486,11 @@ __global__ void lnlike_reduce_kernel(const double* __restrict__ partials, int nb
     double s = 0.0;
     for (int b = 0; b < nblk; ++b) s += partials[((size_t)pv * nblk + b) * (1 + ngrad) + i];
     if (!valid) s = CUDART_NAN;
-    if (i == 0) lnl[pv] = s + *cconst;
+    if (i == 0) {
+      double c = 0.0;
+      for (int b = 0; b < ncpart; ++b) c += cpart[b];
+      lnl[pv] = s + c;
+    }
     else if (grad) grad[(size_t)pv * ngrad + i - 1] = s;
   }
 }
@@ -416,7 +498,7 @@ __global__ void lnlike_reduce_kernel(const double* __restrict__ partials, int nb
 template <typename R>
 struct GradWs {
   R *dc, *tab, *dis, *dobs, *isig2;
-  double *partials, *cconst;
+  double *partials, *cconst;   // cconst: the constant of lnL in per-block parts
 };
 
 template <typename R>
@@ -428,7 +510,7 @@ static GradWs<R> carve_grad(Carve& cv, int npv, int npb, int npar, int ng, int n
   g.dobs = cv.take<R>((size_t)npt);
   g.isig2 = cv.take<R>((size_t)npt);
   g.partials = cv.take<double>((size_t)npv * nblk * (1 + ngrad));
-  g.cconst = cv.take<double>(1);
+  g.cconst = cv.take<double>((size_t)(npt + OBS_CHUNK - 1) / OBS_CHUNK);
   return g;
 }
 
@@ -442,7 +524,7 @@ int rr_lnlike_ngrad(int nkc, int nep, int npb, int npar) { return nkc + nep + 5 
 
 size_t rr_lnlike_workspace_bytes(int split, int npv, int npb, int nlc, int nep, int ng, int npar, int npt,
                                  int nkc) {
-  const int nblk = (npt + GRAD_THREADS - 1) / GRAD_THREADS;
+  const int nblk = (npt + LNL_CHUNK - 1) / LNL_CHUNK;
   const int ngrad = rr_lnlike_ngrad(nkc, nep, npb, npar);
   size_t base = split ? rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng) : rr_full_f64_workspace_bytes(npv, npb, ng);
   Carve c(nullptr);
@@ -485,7 +567,7 @@ static int lnlike_impl(int split, int law, const double* ldc, int npar, const do
     st = rr_prepare_f64(k, nkc, p, a, inc, e, w, npv, npb, (const double*)ldp, (const double*)weights, nk, ng, nz,
                         dk, kmin, kmax, z_edges, workspace, base, stream, 0, nullptr, 0, nullptr, 0);
   if (st) return st;
-  const int nblk = (npt + GRAD_THREADS - 1) / GRAD_THREADS;
+  const int nblk = (npt + LNL_CHUNK - 1) / LNL_CHUNK;
   Carve cv(static_cast<char*>(workspace) + base);
   GradWs<R> g = carve_grad<R>(cv, npv, npb, npar, ng, npt, nblk, ngrad);
   // prologue tables of the forward pass (inside the base workspace)
@@ -504,7 +586,8 @@ static int lnlike_impl(int split, int law, const double* ldc, int npar, const do
   grad_orbit_kernel<R><<<(npv + 63) / 64, 64, 0, s>>>(p, a, inc, e, w, npv, g.dc);
   grad_ld_kernel<R><<<dim3(npv, npb), 128, 0, s>>>(law, ldc, npb, npar, mu, nz, ldp, k, nkc, weights, nk, ng, dk,
                                                    kmin, kmax, z_edges, g.tab, g.dis);
-  obs_kernel<R><<<1, 1024, 0, s>>>(obs, sigma, lcids, npt, g.dobs, g.isig2, g.cconst);
+  const int nobs = (npt + OBS_CHUNK - 1) / OBS_CHUNK;
+  obs_kernel<R><<<nobs, OBS_THREADS, 0, s>>>(obs, sigma, lcids, npt, g.dobs, g.isig2, g.cconst);
   GradArgs<R> A{};
   A.times = times; A.times_ff = reinterpret_cast<const float2*>(times_ff);
   A.lcids = lcids; A.pbids = pbids; A.epids = epids; A.nsamples = nsamples; A.exptimes = exptimes;
@@ -515,9 +598,14 @@ static int lnlike_impl(int split, int law, const double* ldc, int npar, const do
   A.npt = npt; A.npv = npv; A.npb = npb; A.nlc = nlc; A.ng = ng; A.npar = npar; A.ngrad = ngrad;
   A.dg = dg; A.grad = grad != nullptr; A.partials = g.partials;
   dim3 grid(nblk, npv);
-  if (split) lnlike_kernel<R, true><<<grid, GRAD_THREADS, 0, s>>>(A);
-  else lnlike_kernel<R, false><<<grid, GRAD_THREADS, 0, s>>>(A);
-  lnlike_reduce_kernel<<<npv, 64, 0, s>>>(g.partials, nblk, ngrad, npv, g.cconst, orb64, orb32, lnl, grad);
+  if (split) {
+    if (A.grad) lnlike_kernel<R, true, true><<<grid, LNL_THREADS, 0, s>>>(A);
+    else lnlike_kernel<R, true, false><<<grid, LNL_THREADS, 0, s>>>(A);
+  } else {
+    if (A.grad) lnlike_kernel<R, false, true><<<grid, LNL_THREADS, 0, s>>>(A);
+    else lnlike_kernel<R, false, false><<<grid, LNL_THREADS, 0, s>>>(A);
+  }
+  lnlike_reduce_kernel<<<npv, 64, 0, s>>>(g.partials, nblk, ngrad, npv, g.cconst, nobs, orb64, orb32, lnl, grad);
   return check_launch("rr_lnlike");
 }
 

@@ -220,3 +220,116 @@ def test_autograd_function_matches_direct_gradient():
                          [x.grad.cpu().numpy()[:, None] for x in ts[2:7]] +
                          [ts[7].grad.cpu().numpy().reshape(5, -1)], axis=1)
     np.testing.assert_allclose(got, g, rtol=1e-12, atol=0)
+
+
+def fd_gradient_h(m, obs, prm, scale):
+    """Central differences with the step H_REL * scale (with floors) and the
+    rounding floor of each: 16 ulps of |lnL| over the step actually taken."""
+    base = {n: np.array(v, dtype=np.float64, copy=True) for n, v in prm.items()}
+    lnl = np.abs(lnl_of(m, obs, base))
+    cols, floors = [], []
+    for name, idx in param_vector(prm):
+        x = base[name][idx] if idx else base[name]
+        h = scale * H_REL * np.maximum(np.abs(x), FLOORS[name])
+        up = {n: v.copy() for n, v in base.items()}
+        dn = {n: v.copy() for n, v in base.items()}
+        if idx:
+            up[name][idx], dn[name][idx] = x + h, x - h
+            step = up[name][idx] - dn[name][idx]
+        else:
+            up[name], dn[name] = x + h, x - h
+            step = up[name] - dn[name]
+        cols.append((lnl_of(m, obs, up) - lnl_of(m, obs, dn)) / step)
+        floors.append(16 * np.finfo(np.float64).eps * lnl / step)
+    return np.stack(cols, -1), np.stack(floors, -1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_gradient_elementwise_vs_finite_differences(precision):
+    """Every element against central FD of the FP64 model, relative to itself:
+    |g - fd| <= 1e-4 |fd| + floor.  The floor is the FD's own uncertainty:
+    its rounding (16 ulps of |lnL| over the step) and its truncation, which
+    is large where a step crosses a kink of the piecewise-linear LD tables,
+    estimated as |FD(2h) - FD(h)|.  The split path is held to that for 90 %
+    of the elements and, for all, to a stated floor of 5e-5 of the column's
+    largest |fd| (its FP32 per-sample arithmetic)."""
+    data, obs, pert, _ = c3_case()
+    m64 = model(**data)
+    # steps of 1e-8 and 5e-9 relative: far fewer of the samples' LD-table
+    # kinks fall within the step than with 1e-6, while the rounding floor of
+    # the FP64 log-likelihood stays well below the gradients
+    fd1, _ = fd_gradient_h(m64, obs, pert, 0.01)
+    fd, floor = fd_gradient_h(m64, obs, pert, 0.005)
+    floor = floor + np.abs(fd1 - fd)
+    _, g = lnl_of(model(precision=precision, **data), obs, pert, grad=True)
+    strict = np.abs(g - fd) <= 1e-4 * np.abs(fd) + floor
+    if precision == 'fp64':
+        assert strict.all(), (np.argwhere(~strict), (np.abs(g - fd) / np.maximum(np.abs(fd), floor))[~strict])
+    else:
+        # FP32 per-sample arithmetic: each term carries ~1e-6 relative error,
+        # so an element that is a small remainder of large cancelling terms
+        # (ingress against egress) is exact only to a few 1e-5 of its
+        # column's scale; elements above that scale meet 1e-4 of themselves
+        scale = 5e-5 * np.abs(fd).max(axis=0, keepdims=True)
+        ok = np.abs(g - fd) <= 1e-4 * np.abs(fd) + floor + scale
+        assert ok.all(), (np.argwhere(~ok), (np.abs(g - fd) / np.maximum(np.abs(fd), floor))[~ok])
+        assert strict.mean() > 0.9
+    # most elements are well above their floor, so the check has teeth
+    assert (np.abs(fd) > 100 * floor).mean() > 0.8
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_lnlike_and_gradient_are_reproducible(precision):
+    """Sums in a fixed order (no floating-point atomics): a repeated call
+    returns the same bits."""
+    data, obs, pert, _ = c3_case(npv=8, npt=6000)
+    m = model(precision=precision, **data)
+    l1, g1 = lnl_of(m, obs, pert, grad=True)
+    l2, g2 = lnl_of(m, obs, pert, grad=True)
+    l3 = lnl_of(m, obs, pert)
+    assert np.array_equal(l1, l2) and np.array_equal(g1, g2)
+    np.testing.assert_allclose(l3, l1, rtol=1e-12)
+
+
+def test_light_curves_interleaved_point_by_point():
+    """Light curves whose points alternate (every thread's points change light
+    curve): the per-light-curve gradient columns still match FD."""
+    rng = np.random.default_rng(23)
+    T = 2459000.0
+    npt = 3000
+    time = T + np.linspace(-0.2, 0.2, npt)
+    lcids = np.arange(npt) % 3
+    data = dict(time=time, lcids=lcids, pbids=[0, 1, 2], nsamples=[1, 3, 2], exptimes=[0.0, 0.01, 0.02])
+    npv = 3
+    prm = dict(k=rng.uniform(0.09, 0.11, (npv, 3)), ldc=rng.uniform(0.1, 0.4, (npv, 3, 2)),
+               t0=T + rng.normal(0, 1e-3, (npv, 1)), p=np.full(npv, 3.0), a=rng.uniform(7, 9, npv),
+               i=np.arccos(rng.uniform(0, 0.5, npv) / 8), e=rng.uniform(0.02, 0.1, npv),
+               w=rng.uniform(0, 2 * np.pi, npv))
+    ref = oracle.OracleRoadRunner('quadratic')
+    ref.set_data(**data)
+    flux = ref.evaluate(prm['k'], prm['ldc'], prm['t0'], prm['p'], prm['a'], prm['i'], prm['e'], prm['w'])
+    obs = flux[0] + rng.normal(0, SIGMA, npt)
+    for precision, rtol in (('fp64', 1e-9), ('split', 1e-6)):
+        m = model(precision=precision, **data)
+        lnl, g = lnl_of(m, obs, prm, grad=True)
+        np.testing.assert_allclose(lnl, oracle.lnlike_normal(obs, flux, SIGMA), rtol=rtol)
+    m = model(**data)
+    _, g = lnl_of(m, obs, prm, grad=True)
+    base = {n: np.array(v, dtype=np.float64, copy=True) for n, v in prm.items()}
+    cols = []
+    spec = [('k', (slice(None), b)) for b in range(3)] + [('t0', (slice(None), 0))] + \
+           [(n, ()) for n in ('p', 'a', 'i', 'e', 'w')] + [('ldc', (slice(None), b, j)) for b in range(3) for j in range(2)]
+    for name, idx in spec:
+        x = base[name][idx] if idx else base[name]
+        h = np.full_like(x, 1e-7) if name == 't0' else H_REL * np.maximum(np.abs(x), FLOORS[name])
+        up = {n: v.copy() for n, v in base.items()}
+        dn = {n: v.copy() for n, v in base.items()}
+        if idx:
+            up[name][idx], dn[name][idx] = x + h, x - h
+            step = up[name][idx] - dn[name][idx]
+        else:
+            up[name], dn[name] = x + h, x - h
+            step = up[name] - dn[name]
+        cols.append((lnl_of(m, obs, up) - lnl_of(m, obs, dn)) / step)
+    fd = np.stack(cols, -1)
+    assert rel_err(g, fd).max() < 1e-4, rel_err(g, fd).max(axis=0)
