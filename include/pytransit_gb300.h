@@ -329,6 +329,20 @@ int rr_es_f64(const double *times, int npt, const double *k, const double *t0, c
 int rr_lpf_map(const double *pv, int npv, int ldpv, int npb, int ld_start, double tref, double *k, double *t0,
                double *p, double *a, double *inc, double *ldc, void *stream);
 
+/* ---- stated error bounds of the split paths ----------------------------------- */
+
+/* No counterpart in the reference (the reference has one precision): after
+ * rr_prepare_split[_ld] (resp. rr_ts_prepare_split[_ld]) on `workspace`, an
+ * upper bound of |F_split - F_FP64| over all points of each parameter vector,
+ * bound[npv] (FP64, 0 for an invalid vector), and their maximum in
+ * *bound_max if not NULL.  p, a, inc, e, w are the same FP64 parameters. */
+int rr_split_error_bounds(const double *p, const double *a, const double *inc, const double *e, const double *w,
+                          int npv, int npb, int nlc, int nep, int ng, double dg, const void *workspace,
+                          double *bound, double *bound_max, void *stream);
+int rr_ts_split_error_bounds(const double *p, const double *a, const double *inc, const double *e, const double *w,
+                             int npv, int npb, int ng, double dg, int nsamples0, double exptime0,
+                             const void *workspace, double *bound, double *bound_max, void *stream);
+
 /* ---- serving: many requests in one persistent launch ---------------------- */
 
 /* One request of the serving loop (all pointers on the device).
@@ -388,7 +402,9 @@ int rr_serve_flux_split(const rr_serve_request *reqs, const rr_serve_item *items
  * rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng) exceeds that size.
  * It calls no cudaMalloc/cudaFree.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the one
+ * make that first call before any stream capture.  The address is kept per
+ * device and CUDA context: the first call after a device reset (a new
+ * context) looks it up again.  All calls share the one
  * array, which keeps the last call's contents (nothing in it needs clearing:
  * every table is written before it is read); calls that overlap on the GPU,
  * on different streams or host threads, race on it. */

@@ -73,6 +73,8 @@ def _sig(L):
     L.rr_ts_flux_f64.argtypes = [_vp, _i, _vp, _vp, _i, _i, _i, _d, _i, _d, _vp, _vp, _i, _vp]
     L.rr_ts_tables.argtypes = [_vp, _i, _i, _i, _i, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]
     L.rr_ts_tables.restype = None
+    L.rr_split_error_bounds.argtypes = [_vp] * 5 + [_i, _i, _i, _i, _i, _d, _vp, _vp, _vp, _vp]
+    L.rr_ts_split_error_bounds.argtypes = [_vp] * 5 + [_i, _i, _i, _d, _i, _d, _vp, _vp, _vp, _vp]
     for name, args in _EXTRA_SIGNATURES.items():
         if hasattr(L, name):
             getattr(L, name).argtypes = args[0]

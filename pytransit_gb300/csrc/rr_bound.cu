@@ -1,0 +1,203 @@
+// Stated flux-error bounds of the split-precision paths: for every parameter
+// vector, an upper bound of |F_split - F_FP64| over all its points, where
+// F_FP64 is the plain FP64 path (which follows the reference's FP64
+// arithmetic, model_full.py:75-99 and model_trspec.py:72-93, to ~1e-15).
+//
+// The bound is built from the split path's own prologue tables and the FP64
+// parameters, one warp per parameter vector:
+//   * the z error: the FP32 Taylor coefficients against the FP64 jet
+//     recomputed here (the difference itself, not an estimate of it) summed
+//     over the bounding box, |t|^j sum_j |dc_j|, plus the FP32 Horner, the
+//     FP32 sample time and the square root: dz <= sum_j |dc_j| tb^j
+//     + 4u M + u tb V + 4u (1 + k) + 1e-11 V, with u = 2^-24,
+//     M = sum_j |c_j| tb^j and V = sum_j j |c_j| tb^(j-1) (the largest sky
+//     speed), tb the largest |t| a sample of the box reaches;
+//   * the flux's sensitivity to z on every LD-table row j (a sample in row j
+//     has z in [z_j, z_j+1]): |dF/dz| <= (2 min(k, 1) I + A |dI/dz|) / istar
+//     with I <= max(L_j, L_j+1), A <= A(z_j) (the area falls with z) and
+//     |dI/dz| = |L_j+1 - L_j| / (dg (1 + k));
+//   * the deficit's FP32 relative error: (64 + ns) u I A / istar per row (the
+//     FP32 tables, lerp, kite area, disk integral and the sum over the ns
+//     samples);
+//   * the lerp position's rounding: 3u (g / dg) |L_j+1 - L_j| A / istar;
+//   * the FP32 result's own rounding, u.
+// The transmission-spectroscopy bound takes per channel the first-order area
+// A_b <= max(afac A, A + |k_b - kmean| 2 pi kmean) and adds the k-derivative
+// term's change near contact, |k_b - kmean| 2 kmean dkappa I / istar, with
+// dkappa <= sqrt(2 dz / (kmean (1 - kmean))) (kappa_0 has a square-root
+// singularity at the contacts, so this term, not the area, sets the TS bound).
+#include <cmath>
+
+#include "rr_device.cuh"
+#include "rr_internal.h"
+#include "rr_ts.cuh"
+
+namespace rr {
+
+constexpr double BOUND_U = 5.9604644775390625e-8;   // 2^-24
+
+struct BoundArgs {
+  const double *p, *a, *inc, *e, *w;
+  const float *orb, *lc, *ldm;   // split RR: orb32 [npv][ORB32], lc32 [npv][nlc][LC32]; TS: orb [npv][TS_ORB], ch [npv][npb][TS_CH]
+  int npv, npb, nlc, ng, ts, nsamples0;
+  double dg, exptime0;
+  double* bound;                 // [npv]
+  unsigned long long* bound_max; // max over pv (bits of a non-negative double), zeroed by the caller
+};
+
+// The z error of pv on |t| <= tb (lane 0 only): the FP32 coefficients of the
+// record against the FP64 jet.
+__device__ inline double z_error(const BoundArgs& B, int pv, const float* c32, double tb, double kmax) {
+  double c[10];
+  solve2d_conj(B.p[pv], B.a[pv], B.inc[pv], B.e[pv], B.w[pv], c);
+  double dcz = 0.0, M = 0.0, V = 0.0, tp = 1.0;
+  for (int j = 0; j < 5; ++j) {
+    dcz += (fabs((double)c32[j] - c[j]) + fabs((double)c32[5 + j] - c[5 + j])) * tp;
+    M += (fabs(c[j]) + fabs(c[5 + j])) * tp;
+    if (j < 4) V += (j + 1) * (fabs(c[j + 1]) + fabs(c[6 + j])) * tp;
+    tp *= tb;
+  }
+  return dcz + 4 * BOUND_U * M + BOUND_U * tb * V + 4 * BOUND_U * (1.0 + kmax) + 1e-11 * V;
+}
+
+__global__ void __launch_bounds__(128) error_bound_kernel(BoundArgs B) {
+  const int lane = threadIdx.x & 31;
+  const int pv = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (pv >= B.npv) return;   // warp-uniform
+  const unsigned FULL = 0xffffffffu;
+  const double u = BOUND_U;
+  const int ng = B.ng;
+  const double dg = B.dg;
+  double worst = 0.0;
+  if (!B.ts) {
+    const float* o = B.orb + (size_t)pv * ORB32;
+    const bool valid = __float_as_int(o[14]) & FLAG_VALID;
+    if (valid) {
+      const float* L0 = B.lc + (size_t)pv * B.nlc * LC32;
+      double tb = 0.0, kmax = 0.0;
+      for (int lc = 0; lc < B.nlc; ++lc) {
+        const float* r = L0 + (size_t)lc * LC32;
+        tb = fmax(tb, fmax(fabs((double)r[LC_LO]), fabs((double)r[LC_HI])) + 0.5 * r[LC_EXPT]);
+        kmax = fmax(kmax, (double)r[LC_K]);
+      }
+      double dz = 0.0;
+      if (lane == 0) dz = z_error(B, pv, o, tb, kmax);
+      dz = __shfl_sync(FULL, dz, 0);
+      for (int lc = 0; lc < B.nlc; ++lc) {
+        const float* r = L0 + (size_t)lc * LC32;
+        const double k = r[LC_K], inv_is = r[LC_INVIS];
+        if (!isfinite(inv_is)) continue;   // every in-box value is NaN on both paths
+        const int ns = __float_as_int(r[LC_NS]), pb = __float_as_int(r[LC_PB]);
+        const float* L = B.ldm + ((size_t)pv * B.npb + pb) * ng;
+        for (int j = lane; j < ng - 1; j += 32) {
+          const double l0 = L[j], l1 = L[j + 1];
+          const double Lm = fmax(fabs(l0), fabs(l1)), dL = fabs(l1 - l0);
+          float kap;
+          const double A = ccia_star<float>((float)k, (float)(j * dg * (1.0 + k)), kap);
+          const double S = (2.0 * fmin(k, 1.0) * Lm + A * dL / (dg * (1.0 + k))) * fabs(inv_is);
+          const double e = (64 + ns) * u * Lm * A * fabs(inv_is) + S * dz +
+                           3 * u * ((j + 1) * 1.0) * dL * A * fabs(inv_is);
+          worst = fmax(worst, e);
+        }
+      }
+    }
+  } else {
+    const float* o = B.orb + (size_t)pv * TS_ORB;
+    const bool valid = o[15] != 0.0f;
+    if (valid) {
+      const double km = o[12];
+      const double tb = fmax(fabs((double)o[10]), fabs((double)o[11])) + 0.5 * B.exptime0;
+      const float* ch = B.lc + (size_t)pv * B.npb * TS_CH;
+      double afmax = 1.0;
+      for (int b = 0; b < B.npb; ++b) afmax = fmax(afmax, (double)ch[b * TS_CH]);
+      const double kmax = km * sqrt(afmax);
+      double dz = 0.0;
+      if (lane == 0) dz = z_error(B, pv, o, tb, kmax);
+      dz = __shfl_sync(FULL, dz, 0);
+      // kappa_0 near the outer (inner) contact goes as sqrt(2 eps / (k (1 +- k))):
+      // a z error dz moves it by at most sqrt(2 dz / (k (1 - k)))
+      const double dkap = sqrt(2.0 * dz / (km * fmax(1.0 - km, 1e-3)));
+      const int ns = B.nsamples0;
+      for (int b = 0; b < B.npb; ++b) {
+        const double afac = ch[b * TS_CH], dk = fabs((double)ch[b * TS_CH + 1]), inv_is = ch[b * TS_CH + 2];
+        if (!isfinite(inv_is)) continue;
+        const double kb = km * sqrt(afac);
+        const float* L = B.ldm + ((size_t)pv * B.npb + b) * ng;
+        for (int j = lane; j < ng - 1; j += 32) {
+          const double l0 = L[j], l1 = L[j + 1];
+          const double Lm = fmax(fabs(l0), fabs(l1)), dL = fabs(l1 - l0);
+          float kap;
+          const double A0 = ccia_star<float>((float)km, (float)(j * dg * (1.0 + km)), kap);
+          const double A = fmax(afac * A0, A0 + dk * 2.0 * PI * km);
+          const double S = (2.0 * fmin(fmax(kb, km), 1.0) * Lm + A * dL / (dg * (1.0 + km))) * fabs(inv_is);
+          const double e = (64 + ns) * u * Lm * A * fabs(inv_is) + S * dz +
+                           3 * u * ((j + 1) * 1.0) * dL * A * fabs(inv_is) + dk * 2.0 * km * dkap * Lm * fabs(inv_is);
+          worst = fmax(worst, e);
+        }
+      }
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) worst = fmax(worst, __shfl_xor_sync(FULL, worst, off));
+  if (lane == 0) {
+    const double bnd = worst > 0.0 ? worst + u : 0.0;
+    B.bound[pv] = bnd;
+    if (B.bound_max) atomicMax(B.bound_max, (unsigned long long)__double_as_longlong(bnd));
+  }
+}
+
+static int launch_bounds(BoundArgs& B, void* stream) {
+  if (B.npv < 0 || B.npb < 1 || B.ng < 2 || !B.bound || !B.p || !B.a || !B.inc || !B.e || !B.w) return RR_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  if (B.bound_max) {
+    const cudaError_t e = cudaMemsetAsync(B.bound_max, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) {
+      set_cuda_error(e, "rr_error_bounds");
+      return RR_ERR_CUDA;
+    }
+  }
+  if (B.npv == 0) return RR_OK;
+  const unsigned nblk = (unsigned)((B.npv + 3) / 4);
+  error_bound_kernel<<<nblk, 128, 0, s>>>(B);
+  return check_launch("rr_error_bounds");
+}
+
+}  // namespace rr
+
+using namespace rr;
+
+extern "C" {
+
+int rr_split_error_bounds(const double* p, const double* a, const double* inc, const double* e, const double* w,
+                          int npv, int npb, int nlc, int nep, int ng, double dg, const void* workspace,
+                          double* bound, double* bound_max, void* stream) {
+  (void)nep;
+  if (nlc < 1) return RR_ERR_ARG;
+  BoundArgs B{};
+  B.p = p; B.a = a; B.inc = inc; B.e = e; B.w = w;
+  const float *orb = nullptr, *lc = nullptr, *ldm = nullptr;
+  rr_full_split_tables(const_cast<void*>(workspace), npv, npb, nlc, nep, ng, &orb, &lc, &ldm);
+  B.orb = orb; B.lc = lc; B.ldm = ldm;
+  B.npv = npv; B.npb = npb; B.nlc = nlc; B.ng = ng; B.ts = 0; B.dg = dg;
+  B.bound = bound;
+  B.bound_max = reinterpret_cast<unsigned long long*>(bound_max);
+  return launch_bounds(B, stream);
+}
+
+int rr_ts_split_error_bounds(const double* p, const double* a, const double* inc, const double* e, const double* w,
+                             int npv, int npb, int ng, double dg, int nsamples0, double exptime0,
+                             const void* workspace, double* bound, double* bound_max, void* stream) {
+  if (nsamples0 < 1) return RR_ERR_ARG;
+  BoundArgs B{};
+  B.p = p; B.a = a; B.inc = inc; B.e = e; B.w = w;
+  const void *orb = nullptr, *ch = nullptr, *ldm = nullptr;
+  rr_ts_tables(const_cast<void*>(workspace), 1, npv, npb, ng, &orb, &ch, &ldm);
+  B.orb = static_cast<const float*>(orb); B.lc = static_cast<const float*>(ch);
+  B.ldm = static_cast<const float*>(ldm);
+  B.npv = npv; B.npb = npb; B.nlc = 1; B.ng = ng; B.ts = 1; B.dg = dg;
+  B.nsamples0 = nsamples0; B.exptime0 = exptime0;
+  B.bound = bound;
+  B.bound_max = reinterpret_cast<unsigned long long*>(bound_max);
+  return launch_bounds(B, stream);
+}
+
+}  // extern "C"

@@ -11,6 +11,8 @@ namespace rr {
 // Records the CUDA error (if any) of the last launch on this host thread.
 int check_launch(const char* where);
 void set_cuda_error(cudaError_t e, const char* where);
+// Records a message of the library's own (not a CUDA error) for rr_last_cuda_error.
+void set_error_text(const char* where, const char* what);
 
 // LD-means kernel launchers (rr_full.cu); mode 0: rr_full rule, 1: the
 // transmission-spectroscopy rule with kmax_pv, 2: always the 2D table.

@@ -5,6 +5,8 @@
 // synchronise the device) is not acceptable.  Instead of a caller-provided
 // workspace, the per-parameter-vector tables live in a fixed, file-scope
 // device array that every GPU loading this library keeps until process exit.
+#include <cuda.h>   // the driver's context types, for the context check below
+
 #include <mutex>
 
 #include "rr_internal.h"
@@ -18,11 +20,41 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 
 constexpr int MAX_DEVICES = 64;
 static void* g_scratch_addr[MAX_DEVICES] = {};
+static unsigned long long g_scratch_ctx[MAX_DEVICES] = {};
 static std::mutex g_scratch_mutex;
+
+// The id of the current CUDA context (cuCtxGetId, reached through the runtime's
+// driver entry points so that the library links the runtime only), or 0 if it
+// cannot be had.  A device reset, or a primary context released and made
+// again, gives the device a new context id and the module a new address.
+static unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", reinterpret_cast<void**>(&get_current), 12000,
+                                         cudaEnableDefault, &q1) != cudaSuccess || q1 != cudaDriverEntryPointSuccess)
+      get_current = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", reinterpret_cast<void**>(&get_id), 12000, cudaEnableDefault,
+                                         &q2) != cudaSuccess || q2 != cudaDriverEntryPointSuccess)
+      get_id = nullptr;
+    looked_up = true;
+  }
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // Device address of the scratch array on the current device.  In host code
 // the array's name is only a host-side stand-in, so the address is looked up
-// once per device (with that device current) and cached.
+// with the device current, once per device and context, and cached; a call
+// in a context other than the cached one (after a device reset, say) looks it
+// up again.
 static int scratch_address(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -30,9 +62,13 @@ static int scratch_address(void** out) {
     set_cuda_error(e, "rr_full_split_noalloc: cudaGetDevice");
     return RR_ERR_CUDA;
   }
-  if (dev < 0 || dev >= MAX_DEVICES) return RR_ERR_ARG;
+  if (dev < 0 || dev >= MAX_DEVICES) {
+    set_error_text("rr_full_split_noalloc", "device index beyond the 64 devices the scratch cache covers");
+    return RR_ERR_ARG;
+  }
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (g_scratch_addr[dev] == nullptr) {
+  const unsigned long long ctx = current_context_id();
+  if (g_scratch_addr[dev] == nullptr || ctx == 0 || ctx != g_scratch_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) {
@@ -40,6 +76,7 @@ static int scratch_address(void** out) {
       return RR_ERR_CUDA;
     }
     g_scratch_addr[dev] = p;
+    g_scratch_ctx[dev] = current_context_id();   // the lookup has made the context current if it was not
   }
   *out = g_scratch_addr[dev];
   return RR_OK;

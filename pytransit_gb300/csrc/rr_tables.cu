@@ -15,6 +15,10 @@ void set_cuda_error(cudaError_t e, const char* where) {
   snprintf(g_last_error, sizeof(g_last_error), "%s: %s", where, cudaGetErrorString(e));
 }
 
+void set_error_text(const char* where, const char* what) {
+  snprintf(g_last_error, sizeof(g_last_error), "%s: %s", where, what);
+}
+
 int sm_count() {
   constexpr int kMaxDev = 64;
   static int cached[kMaxDev] = {0};

@@ -74,8 +74,10 @@ def _run(model, obs, sigma, k, t0, p, a, i, e, w, ldc, want_grad):
     obs = torch.as_tensor(obs, dtype=torch.float64).to(device).contiguous()
     if obs.numel() != npt:
         raise ValueError(f"obs should have {npt} values")
-    sig = torch.as_tensor(np.broadcast_to(np.asarray(sigma, dtype=np.float64), (nlc,)).copy()).to(device) \
-        if not torch.is_tensor(sigma) else sigma.to(device=device, dtype=torch.float64).expand(nlc).contiguous()
+    if torch.is_tensor(sigma):
+        sig = sigma.to(device=device, dtype=torch.float64).reshape(-1).expand(nlc).contiguous()
+    else:
+        sig = torch.as_tensor(np.broadcast_to(np.asarray(sigma, dtype=np.float64), (nlc,)).copy()).to(device)
     ngrad = L.rr_lnlike_ngrad(nkc, nep, npb, npar)
     wsb = L.rr_lnlike_workspace_bytes(int(split), npv, npb, nlc, nep, model.ng, npar, npt, nkc)
     ws = model._workspace(wsb, device)
@@ -94,14 +96,20 @@ def _run(model, obs, sigma, k, t0, p, a, i, e, w, ldc, want_grad):
     return lnl, g
 
 
-def _as_params(model, k, t0, p, a, i, e, w, ldc):
-    """Shape the parameters as evaluate() does and move them to the device."""
+def _as_params(model, k, t0, p, a, i, e, w, ldc, extra=None):
+    """Shape the parameters as evaluate() does and move them to the device, in
+    one host-to-device copy through the model's pinned staging buffer (with
+    the arrays of `extra`, a dict of float64 arrays, in the same copy)."""
     device = model._cuda_device()
     vals = [x.detach().cpu().numpy() if torch.is_tensor(x) else x for x in (k, t0, p, a, i, e, w)]
     k_, t0_, p_, a_, i_, e_, w_ = model._shape_params(*vals)
     ldc_ = ldc.detach().cpu().numpy() if torch.is_tensor(ldc) else ldc
     ldc3 = model._shape_ldc(ldc_, p_.size, model.npb)
-    return [torch.as_tensor(np.ascontiguousarray(v)).to(device) for v in (k_, t0_, p_, a_, i_, e_, w_, ldc3)]
+    arrays = dict(k=k_, t0=t0_, p=p_, a=a_, i=i_, e=e_, w=w_, ldc=ldc3)
+    arrays.update(extra or {})
+    dev = model._upload({n: np.ascontiguousarray(v, dtype=np.float64) for n, v in arrays.items()}, device)
+    out = [dev[n] for n in ('k', 't0', 'p', 'a', 'i', 'e', 'w', 'ldc')]
+    return (out, {n: dev[n] for n in (extra or {})}) if extra is not None else out
 
 
 def lnlikelihood(model, obs, sigma, k, ldc, t0, p, a, i, e=0.0, w=0.0, grad=False, copy=True):
@@ -110,8 +118,13 @@ def lnlikelihood(model, obs, sigma, k, ldc, t0, p, a, i, e=0.0, w=0.0, grad=Fals
     curve) for each parameter vector; with grad=True also its gradient,
     columns as ``grad_columns``.  Returns numpy arrays (copy=True) or CUDA
     tensors."""
-    k_, t0_, p_, a_, i_, e_, w_, ldc3 = _as_params(model, k, t0, p, a, i, e, w, ldc)
-    lnl, g = _run(model, obs, sigma, k_, t0_, p_, a_, i_, e_, w_, ldc3, grad)
+    extra = {}
+    if not torch.is_tensor(obs):
+        extra['obs'] = np.asarray(obs, dtype=np.float64).reshape(-1)
+    if not torch.is_tensor(sigma):
+        extra['sigma'] = np.broadcast_to(np.asarray(sigma, dtype=np.float64), (model.nlc,)).copy()
+    (k_, t0_, p_, a_, i_, e_, w_, ldc3), dev = _as_params(model, k, t0, p, a, i, e, w, ldc, extra)
+    lnl, g = _run(model, dev.get('obs', obs), dev.get('sigma', sigma), k_, t0_, p_, a_, i_, e_, w_, ldc3, grad)
     if copy:
         lnl = lnl.cpu().numpy()
         g = g.cpu().numpy() if g is not None else None

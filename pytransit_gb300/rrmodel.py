@@ -368,7 +368,7 @@ class RoadRunnerModel(TransitModel):
     def evaluate(self, k: Union[float, ndarray], ldc: Union[ndarray, List], t0: Union[float, ndarray],
                  p: Union[float, ndarray], a: Union[float, ndarray], i: Union[float, ndarray],
                  e: Union[float, ndarray] = 0.0, w: Union[float, ndarray] = 0.0, copy: bool = True,
-                 out=None):
+                 out=None, return_error: bool = False):
         """Evaluate the transit model for one or many parameter vectors.
 
         Returns the modelled flux, [npt] for one parameter vector and
@@ -378,12 +378,62 @@ class RoadRunnerModel(TransitModel):
         [npv, npt] torch tensor (pinned host memory or device) that receives the
         flux; it is filled, synchronised and returned.  In the split path a
         contiguous pinned host float32 tensor is filled in parameter-vector
-        chunks, each copied to the host while the next one is computed."""
+        chunks, each copied to the host while the next one is computed.
+
+        return_error=True returns (flux, bound): the stated maximum absolute
+        flux error of this result against the FP64 model (see
+        ``last_error_bound``)."""
         device = self._cuda_device()
         k, t0, p, a, i, e, w = self._shape_params(k, t0, p, a, i, e, w)
         ldc3 = self._shape_ldc(ldc, p.size, self.npb) if self.ld_law is not None else None
         args = self._upload(dict(k=k, t0=t0, p=p, a=a, i=i, e=e, w=w, ldc=ldc3), device)
-        return self._evaluate_device(args, ldc, out, copy)
+        res = self._evaluate_device(args, ldc, out, copy)
+        return (res, self.last_error_bound) if return_error else res
+
+    # ------------------------------------------------------------------
+    # Stated error of the last result
+    FP64_ERROR_BOUND = 1e-12   # the plain path follows the reference's FP64 arithmetic (measured <= 2e-15)
+
+    def error_bounds(self):
+        """Per parameter vector of the last evaluate(): an upper bound of the
+        absolute flux error against the FP64 model over all its points (numpy
+        float64).  The split path's bound comes from its own tables
+        (rr_split_error_bounds): the FP32 orbit coefficients against the FP64
+        ones, the flux's sensitivity to z on every LD-table row, the FP32
+        deficit and the FP32 result.  Valid until the next evaluate()."""
+        import torch
+        from . import _lib
+        st = getattr(self, '_bound_state', None)
+        if st is None:
+            raise RuntimeError("no evaluation to state an error bound for")
+        if st.get('bounds') is not None:
+            return st['bounds']
+        if not st['split']:
+            st['bounds'] = np.full(st['npv'], self.FP64_ERROR_BOUND)
+            return st['bounds']
+        device = st['device']
+        L = _lib.lib()
+        P = _lib.ptr
+        bnd = torch.empty(st['npv'], dtype=torch.float64, device=device)
+        prm = st['prm']
+        if st.get('ts'):
+            rc = L.rr_ts_split_error_bounds(*(P(prm[n]) for n in ('p', 'a', 'i', 'e', 'w')), st['npv'], st['npb'],
+                                            self.ng, self.dg, st['ns0'], st['ex0'], P(st['ws']), P(bnd), None,
+                                            _lib.stream_ptr(device))
+        else:
+            rc = L.rr_split_error_bounds(*(P(prm[n]) for n in ('p', 'a', 'i', 'e', 'w')), st['npv'], st['npb'],
+                                         st['nlc'], st['nep'], self.ng, self.dg, P(st['ws']), P(bnd), None,
+                                         _lib.stream_ptr(device))
+        _lib.check(rc, "rr_split_error_bounds")
+        st['bounds'] = bnd.cpu().numpy()
+        return st['bounds']
+
+    @property
+    def last_error_bound(self) -> float:
+        """The stated maximum absolute flux error of the last evaluate()'s
+        result against the FP64 model (the largest of ``error_bounds()``)."""
+        b = self.error_bounds()
+        return float(np.nanmax(b)) if b.size else 0.0
 
     def _evaluate_device(self, args, ldc=None, out=None, copy=False):
         """The device half of evaluate: args holds float64 device tensors k[npv,
@@ -459,6 +509,8 @@ class RoadRunnerModel(TransitModel):
                                    P(dd['nsamples']), P(dd['exptimes']), P(istar), self.ng, self.dg, P(ws),
                                    P(res), npt, stream)
         _lib.check(st, "rr_full")
+        self._bound_state = dict(split=split, npv=npv, npb=npb, nlc=nlc, nep=t0.shape[1], ws=ws, device=device,
+                                 prm={n: args[n] for n in ('p', 'a', 'i', 'e', 'w')})
         if user_out is not None:
             if not pipe:
                 src = res if user_out.dtype == res.dtype else res.to(user_out.dtype)

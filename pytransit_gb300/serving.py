@@ -614,6 +614,9 @@ class GpuExecutor:
         self.items_d = torch.zeros(self.MAX_ITEMS * 6 + 8, dtype=torch.int32, device=self.device)
         self.counter = torch.zeros(4, dtype=torch.int32, device=self.device)
         self.free_slots = list(range(self.MAX_REQ - 1, -1, -1))
+        # per slot: the stated error bound of the request holding it
+        self.bound_pin = torch.zeros(self.MAX_REQ, dtype=torch.float64, pin_memory=True)
+        self.bound_np = self.bound_pin.numpy()
         self.graph = None
         self._capture()
 
@@ -664,7 +667,7 @@ class GpuExecutor:
         arrays = [(name, h[key]) for name, key in self._INPUTS]
         parts = [(name, a.nbytes) for name, a in arrays]
         n_in = _layout(parts)[1]
-        parts += [('times_ff', 4 * max(int(L.rr_time_split_floats(npt)), 4))]
+        parts += [('times_ff', 4 * max(int(L.rr_time_split_floats(npt)), 4)), ('bnd', 8 * npv), ('bmax', 8)]
         if req.kind == 'rr':
             nep = h['t0'].shape[1]
             wsb = int(L.rr_full_split_workspace_bytes(npv, npb, nlc, nep, ng))
@@ -765,6 +768,21 @@ class GpuExecutor:
                     d['exptime0'] = np.float32(h['exptimes'][0])
                     d['dg'], d['inv_dg'] = m.dg, np.float32(1.0 / m.dg)
                     self._dirty.add(slot)
+            # the request's stated error bound (largest over its parameter
+            # vectors), copied to its host slot behind the set-up
+            if 'slot' not in req.state:
+                req.state['slot'] = self.free_slots.pop()
+            bslot = req.state['slot']
+            prm = [P[n] for n in ('p', 'a', 'i', 'e', 'w')]
+            if req.kind == 'rr':
+                rc = L.rr_split_error_bounds(*prm, npv, npb, nlc, h['t0'].shape[1], ng, m.dg, P['ws'], P['bnd'],
+                                             P['bmax'], sp)
+            else:
+                rc = L.rr_ts_split_error_bounds(*prm, npv, npb, ng, m.dg, int(h['nsamples'][0]),
+                                                float(h['exptimes'][0]), P['ws'], P['bnd'], P['bmax'], sp)
+            self._lib.check(rc, "rr_error_bounds")
+            self.bound_pin[bslot:bslot + 1].copy_(buf[off['bmax']:off['bmax'] + 8].view(torch.float64),
+                                                  non_blocking=True)
         ready = torch.cuda.Event()
         ready.record(self.setup_stream)
         if stage is self.ring.buf:
@@ -896,6 +914,7 @@ class GpuExecutor:
         if ev is None or not ev.query():
             return None
         req.state['copy_done'] = True
+        req.state['error_bound'] = float(self.bound_np[req.state['slot']])
         out = req.state['host_out']
         return out if self.result == 'device' else out.numpy()
 

@@ -22,13 +22,15 @@ class TransmissionSpectroscopyModel(RoadRunnerModel):
 
     def evaluate(self, k: Union[float, ndarray], ldc: Union[ndarray, List], t0: Union[float, ndarray],
                  p: Union[float, ndarray], a: Union[float, ndarray], i: Union[float, ndarray],
-                 e: Union[float, ndarray] = 0.0, w: Union[float, ndarray] = 0.0, copy: bool = True):
+                 e: Union[float, ndarray] = 0.0, w: Union[float, ndarray] = 0.0, copy: bool = True,
+                 return_error: bool = False):
         """Transit model for npb channels sharing one orbit.
 
         k: [npv, npb] radius ratios; ldc: [npv, npb, ncoef] (or [npb, ncoef]
         for one parameter vector); t0, p, a, i, e, w: one value per parameter
         vector.  Returns flux[npv, npb, npt] (numpy float64 with copy=True,
-        else the CUDA tensor)."""
+        else the CUDA tensor); with return_error=True (flux, bound), the
+        stated maximum absolute flux error against the FP64 model."""
         import torch
         from . import _lib
         device = self._cuda_device()
@@ -101,9 +103,11 @@ class TransmissionSpectroscopyModel(RoadRunnerModel):
                 st = L.rr_ts_f64(P(dd['time']), npt, *common)
             _lib.check(st, "rr_ts")
         out = out[:, :, :npt]
+        self._bound_state = dict(split=split, ts=True, npv=npv, npb=npb, ns0=ns0, ex0=ex0, ws=ws, device=device,
+                                 prm={n: args[n] for n in ('p', 'a', 'i', 'e', 'w')})
         if copy:
-            return out.to(torch.float64).cpu().numpy()
-        return out
+            out = out.to(torch.float64).cpu().numpy()
+        return (out, self.last_error_bound) if return_error else out
 
     def _host_ld(self, ldc3, npv, npb, device, dt):
         import torch
@@ -120,8 +124,8 @@ class TransmissionSpectroscopyModel(RoadRunnerModel):
         istar = np.require(np.broadcast_to(np.asarray(istar, np.float64), (npv, npb)), requirements='CW')
         return (torch.as_tensor(ldp).to(device=device, dtype=dt), torch.as_tensor(istar).to(device=device, dtype=dt))
 
-    def __call__(self, k, ldc, t0, p, a, i, e=0.0, w=0.0, copy: bool = True):
-        return self.evaluate(k, ldc, t0, p, a, i, e, w, copy)
+    def __call__(self, k, ldc, t0, p, a, i, e=0.0, w=0.0, copy: bool = True, return_error: bool = False):
+        return self.evaluate(k, ldc, t0, p, a, i, e, w, copy, return_error)
 
 
 TSModel = TransmissionSpectroscopyModel

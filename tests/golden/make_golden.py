@@ -390,8 +390,41 @@ def case_eclipse():
     save("eclipse", **out)
 
 
+def case_taylor_orbit():
+    """The reference's own Taylor orbit (pytransit/orbits/taylor_z.py): the
+    finite-difference velocity, acceleration, jerk and snap at mid-transit
+    (vajs_from_paiew), z over the transit window (z_taylor_v) and the contact
+    points (find_contact_point), independent of the meepmeep restatement the
+    RoadRunner fixtures run on."""
+    import types
+    orbits = types.ModuleType("pytransit.orbits")
+    orbits.__path__ = [os.path.join(REF, "pytransit", "orbits")]
+    sys.modules["pytransit.orbits"] = orbits
+    from pytransit.orbits import taylor_z as tz
+    rng = np.random.default_rng(71)
+    n = 48
+    p = rng.uniform(0.5, 15.0, n)
+    a = rng.uniform(3.0, 20.0, n)
+    b = rng.uniform(0.0, 0.9, n)
+    inc = np.arccos(b / a)
+    e = np.where(np.arange(n) % 2 == 0, 0.0, rng.uniform(0.0, 0.3, n))
+    w = rng.uniform(0.0, 2 * np.pi, n)
+    k = rng.uniform(0.05, 0.15, n)
+    tt = np.linspace(-1.0, 1.0, 401)       # in units of the half-window
+    times, z, t14 = np.zeros((n, tt.size)), np.zeros((n, tt.size)), np.zeros((n, 2))
+    vajs = np.zeros((n, 9))
+    for j in range(n):
+        v = tz.vajs_from_paiew(p[j], a[j], inc[j], e[j], w[j])
+        vajs[j] = v
+        t14[j] = [tz.find_contact_point(k[j], 1, *v), tz.find_contact_point(k[j], 4, *v)]
+        half = 1.2 * max(abs(t14[j, 0]), abs(t14[j, 1]))
+        times[j] = tt * half
+        z[j] = tz.z_taylor_v(times[j], 0.0, p[j], *v)
+    save("taylor_orbit", p=p, a=a, inc=inc, e=e, w=w, k=k, times=times, z=z, t14=t14, vajs=vajs)
+
+
 if __name__ == "__main__":
     for f in (case_tables, case_c0, case_multi, case_power2, case_laws, case_user_ld, case_klims,
-              case_simple, case_ts, case_ma_quadratic, case_lpf_map, case_eclipse):
+              case_simple, case_ts, case_ma_quadratic, case_lpf_map, case_eclipse, case_taylor_orbit):
         print(f.__name__)
         f()

@@ -245,3 +245,45 @@ def test_eclipse_reference_test_properties():
     assert abs(f.max() - np.pi * 0.01) < 1e-6
     assert f[np.argmin(np.abs(times - 1.0))] < np.pi * 0.01 - 1e-4
     assert f.min() < 1e-3
+
+
+def test_orbit_restatement_against_the_references_taylor_orbit(golden):
+    """The restated meepmeep orbit layer (shared by the golden shim, the oracle
+    and the CUDA kernels) against the reference's own Taylor orbit,
+    pytransit/orbits/taylor_z.py (fixture from tests/golden/make_golden.py):
+    the Taylor coefficients against vajs_from_paiew (finite differences of the
+    exact Kepler positions), z over the transit window against z_taylor_v, and
+    the contact points against find_contact_point.
+
+    z agrees to 1e-6 over 48 orbits, eccentric ones included: the difference
+    is the truncation of the reference's finite differences (dt = 0.02 d), and
+    with |dF/dz| <= 2k I / istar it moves the flux by at most ~1e-7.
+    find_contact_point folds its trial times with a 1-day period
+    (z_taylor_s(t, 0.0, 1.0, ...)), so its contacts beyond +-0.5 d are not
+    contacts; those are skipped (RoadRunner's box comes from meepmeep's
+    bounding_box, restated without the fold)."""
+    g = golden("taylor_orbit")
+    n = g["p"].size
+    dz = np.zeros(n)
+    compared = 0
+    for j in range(n):
+        c = oracle.solve2d(0.0, g["p"][j], g["a"][j], g["inc"][j], g["e"][j], g["w"][j]).ravel()
+        v = g["vajs"][j]   # y0, vx, vy, ax, ay, jx, jy, sx, sy
+        mine = [c[5], c[1], c[6], 2 * c[2], 2 * c[7], 6 * c[3], 6 * c[8], 24 * c[4], 24 * c[9]]
+        # y0 is exact on both sides; the reference's derivatives carry the
+        # truncation of its 7-point stencils, largest for the fastest orbits
+        np.testing.assert_allclose(mine[0], v[0], rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(mine[1:3], v[1:3], rtol=1e-4, atol=1e-6 * abs(v[1]))
+        np.testing.assert_allclose(mine[3:], v[3:], rtol=2e-2, atol=1e-3 * abs(v[1]))
+        z = np.array([oracle.sep_c(t, c.reshape(2, 5)) for t in g["times"][j]])
+        dz[j] = np.abs(z - g["z"][j]).max()
+        t1, t4 = oracle.bounding_box(g["k"][j], c.reshape(2, 5))
+        for mine_t, ref_t in ((t1, g["t14"][j, 0]), (t4, g["t14"][j, 1])):
+            if abs(ref_t) < 0.45:
+                assert abs(mine_t - ref_t) < 2e-6
+                compared += 1
+    assert dz.max() < 1e-6
+    assert compared >= 80
+    # the flux consequence: |dF| <= max|dF/dz| |dz|, |dF/dz| <= 2 k max(I) / istar (quadratic LD, u = (0.4, 0.2))
+    istar = 2 * np.pi / 12 * (-2 * 0.4 - 0.2 + 6)
+    assert (2 * g["k"].max() / istar * dz.max()) < 2e-7
