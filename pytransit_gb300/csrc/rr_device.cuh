@@ -92,6 +92,24 @@ __device__ __forceinline__ float kite_star_f32(float k, float z) {
   return 1.0f * 1.0f * k1 + k * k * k0 - a_kite;
 }
 
+// kite_star_f32 for k <= 1/4 with one arctangent: the star's half-angle
+// kappa1 (< pi/2 for k < 1) has sin(kappa1) = h, the half-chord, and the kite
+// of diagonals z and 2h has area a_kite = z h, so kappa1 = asin(a_kite / z)
+// with h <= k <= 1/4, where the Maclaurin series of arcsine to h^11,
+//   asin h = h (1 + h^2/6 + 3h^4/40 + 5h^6/112 + 35h^8/1152 + 63h^10/2816),
+// has a remainder below 1e-9 relative (the next term is 231 h^12 / 13312).
+__device__ __forceinline__ float kite_star_f32_smallk(float k, float z) {
+  const float a = fmaxf(1.0f, k), b = fminf(1.0f, k);
+  const float x = fmaxf(a, z), t = fminf(a, z);
+  const float y = fmaxf(b, t), w = fminf(b, t);
+  const float a_kite = 0.5f * sqrtf((x + (y + w)) * (w - (x - y)) * (w + (x - y)) * (x + (y - w)));
+  const float k0 = atan2f(2.0f * a_kite, (k - 1.0f) * (k + 1.0f) + z * z);
+  const float h = a_kite / z, h2 = h * h;
+  const float k1 = h * fmaf(h2, fmaf(h2, fmaf(h2, fmaf(h2, fmaf(h2, 63.0f / 2816.0f, 35.0f / 1152.0f), 5.0f / 112.0f),
+                                                  3.0f / 40.0f), 1.0f / 6.0f), 1.0f);
+  return k1 + k * k * k0 - a_kite;
+}
+
 // The same area with its partial derivatives: dA/dk = 2 k kappa0 (the
 // reference's dfdk, common.py:105-114) and dA/dz = -2 A_kite / z (its dfdb,
 // common.py:117-128).

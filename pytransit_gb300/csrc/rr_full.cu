@@ -784,8 +784,12 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
         if (!__ballot_sync(FULL, limb >> q & 1u)) continue;  // warp-uniform
         const bool lm = limb >> q & 1u;
         const float lerp = fmaf(frq[q], l1q[q] - l0q[q], l0q[q]);
-        if (k < 1.0f) {                                    // tile-uniform
+        if (k <= 0.25f) {                                  // tile-uniform
           const float zz = lm ? zq[q] : 1.0f;              // an in-range z for the other lanes
+          const float a = kite_star_f32_smallk(k, zz);
+          res[q] = lm ? 1.0f - (lerp * a) * invis : res[q];
+        } else if (k < 1.0f) {                             // tile-uniform
+          const float zz = lm ? zq[q] : 1.0f;
           const float a = kite_star_f32(k, zz);
           res[q] = lm ? 1.0f - (lerp * a) * invis : res[q];
         } else if (lm) {
