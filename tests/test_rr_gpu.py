@@ -148,7 +148,8 @@ def test_oracle_parity_bjd(ns, exptime, ecc):
 
 def test_split_vs_fp64_long_baseline():
     """Split vs FP64 over a 1000-day baseline at 30-min cadence with 10
-    supersamples, power-2 LD, eccentric orbits (the precision workload's shape)."""
+    supersamples, power-2 LD, eccentric orbits (the precision workload's
+    shape), and both against the oracle on a seeded 64-pv subset."""
     rng = np.random.default_rng(7)
     npv = 512
     npts = np.exp(rng.uniform(np.log(500), np.log(50000), 16)).astype(int)
@@ -171,6 +172,13 @@ def test_split_vs_fp64_long_baseline():
         out[precision] = m.evaluate(k, ldc, t0, p, a, inc, e, w)
     assert max_err(out["split"], out["fp64"]) <= 1e-6
     assert np.sum(out["fp64"] < 1) > 1000   # the case does exercise in-transit points
+    # a seeded subset of the population against the oracle, on all the times
+    sub = np.sort(rng.choice(npv, 64, replace=False))
+    ref = oracle.OracleRoadRunner('power-2')
+    ref.set_data(**data)
+    want = ref.evaluate(k[sub], ldc[sub], t0[sub], p[sub], a[sub], inc[sub], e[sub], w[sub])
+    assert max_err(out["fp64"][sub], want) <= TOL["fp64"]
+    assert max_err(out["split"][sub], want) <= TOL["split"]
 
 
 @pytest.mark.parametrize("precision", ["fp64", "split"])
