@@ -475,7 +475,7 @@ def bench_c3(torch, device, steps=10):
         err = (np.abs(g - fd) / (1e-4 * np.abs(fd) + fl))[fin]
         big = fin & (np.abs(fd) > 100 * fl)
         fd_check[prec] = {"max_err_over_bound": float(err.max()), "elements_within_bound": float((err <= 1).mean()),
-                          "max_rel_err_where_fd_above_100_floors": float((np.abs(g - fd) / np.abs(fd))[big].max()),
+                          "max_rel_err_where_fd_above_100_floors": float((np.abs(g - fd)[big] / np.abs(fd)[big]).max()),
                           "max_abs_err_over_column_scale": float((np.abs(g - fd) / colmax)[fin].max())}
     fd_check["elements_without_central_difference"] = int((~fin).sum())
     # a repeated call gives the same bits (sums in a fixed order)
@@ -500,23 +500,70 @@ def bench_c3(torch, device, steps=10):
 
 
 def bench_eclipse(torch, device, data, prm, steps=3):
-    """The secondary-eclipse model (FP64) on the default workload's data and
-    population (8192 pv x 19,700 times): model points/s."""
+    """The secondary-eclipse model on the default workload's data and
+    population (8192 pv x 19,700 times), FP64 and split: model points/s
+    (CUDA events, parameters uploaded each call) and the split path's max
+    |dF| against FP64."""
     from pytransit_gb300 import EclipseModel
-    m = EclipseModel(device=device)
-    m.set_data(data["time"], lcids=data["lcids"], pbids=data["pbids"])
     args = (prm["k"][:, 0], prm["t0"], prm["p"], prm["a"], prm["i"], prm["e"], prm["w"])
-    m.evaluate(*args, copy=False)
+    res, outs = {}, {}
+    for prec, n in (("fp64", steps), ("split", 10 * steps)):
+        m = EclipseModel(precision=prec, device=device)
+        m.set_data(data["time"], lcids=data["lcids"], pbids=data["pbids"])
+        m.evaluate(*args, copy=False)
+        stream = torch.cuda.current_stream(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        e0.record(stream)
+        for _ in range(n):
+            out = m.evaluate(*args, copy=False)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        res[prec] = e0.elapsed_time(e1) / n
+        outs[prec] = out
+    # the split step through the C ABI with the parameters already in HBM
+    from pytransit_gb300 import _lib
+    from pytransit_gb300.eclipse import _L
+    m = EclipseModel(precision='split', device=device)
+    m.set_data(data["time"], lcids=data["lcids"], pbids=data["pbids"])
+    dd = m._device_data(device)
+    npv = prm["p"].size
+    g = m._upload(dict(k=np.ascontiguousarray(prm["k"][:, 0]), t0=prm["t0"], p=prm["p"], a=prm["a"], i=prm["i"],
+                       e=prm["e"], w=prm["w"], rstar=np.ones(npv)), device)
+    L, P = _L(), _lib.ptr
+    wsb = L.rr_eclipse_split_workspace_bytes(npv, m.nlc, 1)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=device)
+    dev_out = torch.empty((npv, m.npt), dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    def step():
+        _lib.check(L.rr_eclipse_split(P(dd['times_ff']), dd['t_ref'], dd['t_absmax'], m.npt, P(g['k']), P(g['t0']),
+                                      1, P(g['p']), P(g['a']), P(g['i']), P(g['e']), P(g['w']), P(g['rstar']), npv,
+                                      m.nlc, P(dd['lcids']), P(dd['epids']), P(dd['nsamples']), P(dd['exptimes']),
+                                      P(ws), wsb, P(dev_out), m.npt, _lib.stream_ptr(device)), "rr_eclipse_split")
+    for _ in range(3):
+        step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize(device)
-    t = time.perf_counter()
-    for _ in range(steps):
-        out = m.evaluate(*args, copy=False)
+    e0.record(stream)
+    for _ in range(20):
+        step()
+    e1.record(stream)
     torch.cuda.synchronize(device)
-    dt = (time.perf_counter() - t) / steps
+    dev_ms = e0.elapsed_time(e1) / 20
+    peak, _ = measured_peaks()
     k2 = torch.as_tensor(np.pi * prm["k"][:, :1] ** 2).to(device)
-    return {"workload": "EclipseModel.evaluate(copy=False), 8192 pv x 19700 times, FP64, parameters uploaded each "
-                        "call", "points_per_s": out.numel() / dt, "ms": dt * 1e3,
-            "in_eclipse_fraction": float((out < k2 - 1e-12).double().mean().item())}
+    npts = outs["fp64"].numel()
+    dmax = float((outs["split"].double() - outs["fp64"]).abs().max().item())
+    return {"workload": "EclipseModel.evaluate(copy=False), 8192 pv x 19700 times, parameters uploaded each call, "
+                        "CUDA events", "points_per_s": npts / (res["fp64"] * 1e-3), "ms": res["fp64"],
+            "split_points_per_s": npts / (res["split"] * 1e-3), "split_ms": res["split"],
+            "split_over_fp64": res["fp64"] / res["split"], "max_abs_dF_split_vs_fp64": dmax,
+            "split_device_resident": {"ms_per_step": dev_ms, "points_per_s": npts / (dev_ms * 1e-3),
+                                      "output_frac_of_hbm": 4.0 * npts / (dev_ms * 1e-3) / (peak * 1e9),
+                                      "timed": "rr_eclipse_split (prologue + flux) through the C ABI, inputs in "
+                                               "HBM, CUDA events"},
+            "in_eclipse_fraction": float((outs["fp64"] < k2 - 1e-12).double().mean().item())}
 
 
 class C4Mix:
@@ -602,7 +649,14 @@ def serve_run(srv, reqs, rate, seed=5):
             "latency_p99_first_half_s": p99(lat[:half]), "latency_p99_second_half_s": p99(lat[half:]),
             "queued_at_end_of_arrivals": load_end["queued"], "active_at_end_of_arrivals": load_end["active"],
             "admitted_bytes_at_end_of_arrivals": load_end["admitted_bytes"],
-            "steps": st["steps"] - st0["steps"], "bypassed": st["bypassed"] - st0["bypassed"]}
+            "steps": st["steps"] - st0["steps"], "bypassed": st["bypassed"] - st0["bypassed"],
+            # where the wall time went: device time of the batched steps, and
+            # the scheduler thread's time in admission + set-up, step issue and
+            # completion polling
+            "gpu_step_busy": (st["gpu_step_s"] - st0["gpu_step_s"]) / (t_end - t_start),
+            "host_admit_busy": (st["admit_s"] - st0["admit_s"]) / (t_end - t_start),
+            "host_step_busy": (st["step_s"] - st0["step_s"]) / (t_end - t_start),
+            "host_poll_busy": (st["poll_s"] - st0["poll_s"]) / (t_end - t_start)}
 
 
 def sustained(run):
@@ -681,7 +735,8 @@ def serve_suite(torch, device, rate=2000.0, duration_s=5.0, probe_s=2.5, max_pro
         probes.append({k: run[k] for k in ("offered_req_per_s", "achieved_req_per_s", "latency_p50_s",
                                             "latency_p99_s", "latency_p99_first_half_s",
                                             "latency_p99_second_half_s", "queued_at_end_of_arrivals",
-                                            "points_per_s")})
+                                            "points_per_s", "gpu_step_busy", "host_admit_busy",
+                                            "host_step_busy", "host_poll_busy")})
         good = sustained(run)
         probes[-1]["sustained"] = good
         if good:

@@ -318,6 +318,24 @@ int rr_es_f64(const double *times, int npt, const double *k, const double *t0, c
               const double *inc, const double *e, const double *w, const double *rstar, const double *fratio,
               int npv, int npb, int nsamples0, double exptime0, void *workspace, size_t workspace_bytes,
               double *flux, int ldflux, void *stream);
+/* Split precision of the two (same models, same arguments as the FP64 entry
+ * points, FP32 output): times_ff / t_ref / t_absmax from rr_time_split; the
+ * FP64 per-pv prologue (eclipse shift, light travel time, Taylor jet) is
+ * rounded to FP32 records; each point's time is folded exactly in FP32 pairs
+ * and its samples are evaluated in FP32.  Tiles of 128 points whose time
+ * range reaches no eclipse window are runs of stores of pi k^2 (eclipse) or 1
+ * (ES).  rr_es_split treats every point as one light curve (nsamples0,
+ * exptime0), as esmodel does. */
+size_t rr_eclipse_split_workspace_bytes(int npv, int nlc, int npb);
+int rr_eclipse_split(const float *times_ff, double t_ref, double t_absmax, int npt, const double *k,
+                     const double *t0, int ldt0, const double *p, const double *a, const double *inc,
+                     const double *e, const double *w, const double *rstar, int npv, int nlc, const int32_t *lcids,
+                     const int32_t *epids, const int32_t *nsamples, const double *exptimes, void *workspace,
+                     size_t workspace_bytes, float *flux, int ldflux, void *stream);
+int rr_es_split(const float *times_ff, double t_ref, double t_absmax, int npt, const double *k, const double *t0,
+                const double *p, const double *a, const double *inc, const double *e, const double *w,
+                const double *rstar, const double *fratio, int npv, int npb, int nsamples0, double exptime0,
+                void *workspace, size_t workspace_bytes, float *flux, int ldflux, void *stream);
 
 /* ---- sampler parameter mapping -------------------------------------------- */
 
@@ -385,6 +403,39 @@ void rr_full_split_tables(void *workspace, int npv, int npb, int nlc, int nep, i
  * returns at launch. */
 int rr_serve_flux_split(const rr_serve_request *reqs, const rr_serve_item *items, const int *nitems, int *counter,
                         int nblocks, void *stream);
+
+/* The set-up of one served request (no counterpart in the reference): every
+ * field is 8 bytes.  stage -> dst (n_in bytes) is the host-to-device copy of
+ * the request's inputs (stage in pinned memory); the other pointers are
+ * device addresses of those inputs and of the request's own tables (times_ff,
+ * ldp/istar for RoadRunner, ws, bnd[npv], bmax) and output; mu, basis,
+ * weights, z_edges are the model's tables; desc (pinned, may be NULL) receives
+ * the request's descriptor for rr_serve_flux_split, bound_host (pinned, may
+ * be NULL) its stated error bound. */
+typedef struct {
+  const void *stage;
+  void *dst;
+  int64_t n_in;
+  const double *time;
+  const int32_t *lcids, *pbids, *epids, *nsamples;
+  const double *exptimes, *k, *t0, *p, *a, *inc, *e, *w, *ldc;
+  float *times_ff, *ldp, *istar;
+  void *ws;
+  double *bnd, *bmax;
+  float *flux;
+  const double *mu;
+  const float *basis, *weights;
+  const double *z_edges;
+  int64_t npt, npv, nlc, npb, nep, nkc, npar, law, nb, nk, nz, ng, ldflux, wsb, nsamples0;
+  double t_ref, t_abs, dk, kmin, kmax, dg, exptime0;
+  double *bound_host;
+  rr_serve_request *desc;
+} rr_serve_setup_args;
+/* kind 0: RoadRunner (rr_time_split, rr_prepare_split_ld, rr_split_error_bounds);
+ * kind 1: transmission spectroscopy (rr_time_split, rr_ts_prepare_split_ld,
+ * rr_ts_split_error_bounds); all enqueued on stream. */
+int rr_serve_setup(int kind, const rr_serve_setup_args *args, void *stream);
+void rr_serve_setup_args_size(int *size);
 
 /* ---- no-allocation variant ------------------------------------------------- */
 

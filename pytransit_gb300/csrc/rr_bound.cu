@@ -60,15 +60,21 @@ __device__ inline double z_error(const BoundArgs& B, int pv, const float* c32, d
   return dcz + 4 * BOUND_U * M + BOUND_U * tb * V + 4 * BOUND_U * (1.0 + kmax) + 1e-11 * V;
 }
 
+// Per-row terms in FP32 (the FP64 rate of this GPU is 1/64 of its FP32
+// rate): every term is a sum of products of non-negative values, so its FP32
+// value is within 16 ulps of the exact one and the result is raised by
+// BOUND_SAFETY.  The z error dz is computed in FP64 (z_error) and rounded up.
+constexpr float BOUND_SAFETY = 1.0f + 1e-4f;
+
 __global__ void __launch_bounds__(128) error_bound_kernel(BoundArgs B) {
   const int lane = threadIdx.x & 31;
   const int pv = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   if (pv >= B.npv) return;   // warp-uniform
   const unsigned FULL = 0xffffffffu;
-  const double u = BOUND_U;
+  const float u = (float)BOUND_U;
   const int ng = B.ng;
-  const double dg = B.dg;
-  double worst = 0.0;
+  const float dg = (float)B.dg;
+  float worst = 0.0f;
   if (!B.ts) {
     const float* o = B.orb + (size_t)pv * ORB32;
     const bool valid = __float_as_int(o[14]) & FLAG_VALID;
@@ -80,24 +86,25 @@ __global__ void __launch_bounds__(128) error_bound_kernel(BoundArgs B) {
         tb = fmax(tb, fmax(fabs((double)r[LC_LO]), fabs((double)r[LC_HI])) + 0.5 * r[LC_EXPT]);
         kmax = fmax(kmax, (double)r[LC_K]);
       }
-      double dz = 0.0;
-      if (lane == 0) dz = z_error(B, pv, o, tb, kmax);
-      dz = __shfl_sync(FULL, dz, 0);
+      double dz64 = 0.0;
+      if (lane == 0) dz64 = z_error(B, pv, o, tb, kmax);
+      const float dz = __double2float_ru(__shfl_sync(FULL, dz64, 0));
       for (int lc = 0; lc < B.nlc; ++lc) {
         const float* r = L0 + (size_t)lc * LC32;
-        const double k = r[LC_K], inv_is = r[LC_INVIS];
+        const float k = r[LC_K], inv_is = fabsf(r[LC_INVIS]);
         if (!isfinite(inv_is)) continue;   // every in-box value is NaN on both paths
         const int ns = __float_as_int(r[LC_NS]), pb = __float_as_int(r[LC_PB]);
         const float* L = B.ldm + ((size_t)pv * B.npb + pb) * ng;
+        const float gz = dg * (1.0f + k), inv_gz = 1.0f / gz, k2 = 2.0f * fminf(k, 1.0f);
+        const float cr = (64 + ns) * u;
         for (int j = lane; j < ng - 1; j += 32) {
-          const double l0 = L[j], l1 = L[j + 1];
-          const double Lm = fmax(fabs(l0), fabs(l1)), dL = fabs(l1 - l0);
+          const float l0 = L[j], l1 = L[j + 1];
+          const float Lm = fmaxf(fabsf(l0), fabsf(l1)), dL = fabsf(l1 - l0);
           float kap;
-          const double A = ccia_star<float>((float)k, (float)(j * dg * (1.0 + k)), kap);
-          const double S = (2.0 * fmin(k, 1.0) * Lm + A * dL / (dg * (1.0 + k))) * fabs(inv_is);
-          const double e = (64 + ns) * u * Lm * A * fabs(inv_is) + S * dz +
-                           3 * u * ((j + 1) * 1.0) * dL * A * fabs(inv_is);
-          worst = fmax(worst, e);
+          const float ai = ccia_star<float>(k, (float)j * gz, kap) * inv_is;
+          const float S = k2 * Lm * inv_is + ai * dL * inv_gz;
+          const float e = cr * Lm * ai + S * dz + 3.0f * u * (float)(j + 1) * dL * ai;
+          worst = fmaxf(worst, e);
         }
       }
     }
@@ -105,41 +112,47 @@ __global__ void __launch_bounds__(128) error_bound_kernel(BoundArgs B) {
     const float* o = B.orb + (size_t)pv * TS_ORB;
     const bool valid = o[15] != 0.0f;
     if (valid) {
-      const double km = o[12];
+      const float km = o[12];
       const double tb = fmax(fabs((double)o[10]), fabs((double)o[11])) + 0.5 * B.exptime0;
       const float* ch = B.lc + (size_t)pv * B.npb * TS_CH;
-      double afmax = 1.0;
-      for (int b = 0; b < B.npb; ++b) afmax = fmax(afmax, (double)ch[b * TS_CH]);
-      const double kmax = km * sqrt(afmax);
-      double dz = 0.0;
-      if (lane == 0) dz = z_error(B, pv, o, tb, kmax);
-      dz = __shfl_sync(FULL, dz, 0);
+      float afmax = 1.0f;
+      for (int b = lane; b < B.npb; b += 32) afmax = fmaxf(afmax, ch[b * TS_CH]);
+      for (int off = 16; off > 0; off >>= 1) afmax = fmaxf(afmax, __shfl_xor_sync(FULL, afmax, off));
+      const double kmax = (double)km * sqrt((double)afmax);
+      double dz64 = 0.0;
+      if (lane == 0) dz64 = z_error(B, pv, o, tb, kmax);
+      dz64 = __shfl_sync(FULL, dz64, 0);
+      const float dz = __double2float_ru(dz64);
       // kappa_0 near the outer (inner) contact goes as sqrt(2 eps / (k (1 +- k))):
       // a z error dz moves it by at most sqrt(2 dz / (k (1 - k)))
-      const double dkap = sqrt(2.0 * dz / (km * fmax(1.0 - km, 1e-3)));
-      const int ns = B.nsamples0;
-      for (int b = 0; b < B.npb; ++b) {
-        const double afac = ch[b * TS_CH], dk = fabs((double)ch[b * TS_CH + 1]), inv_is = ch[b * TS_CH + 2];
-        if (!isfinite(inv_is)) continue;
-        const double kb = km * sqrt(afac);
-        const float* L = B.ldm + ((size_t)pv * B.npb + b) * ng;
-        for (int j = lane; j < ng - 1; j += 32) {
-          const double l0 = L[j], l1 = L[j + 1];
-          const double Lm = fmax(fabs(l0), fabs(l1)), dL = fabs(l1 - l0);
-          float kap;
-          const double A0 = ccia_star<float>((float)km, (float)(j * dg * (1.0 + km)), kap);
-          const double A = fmax(afac * A0, A0 + dk * 2.0 * PI * km);
-          const double S = (2.0 * fmin(fmax(kb, km), 1.0) * Lm + A * dL / (dg * (1.0 + km))) * fabs(inv_is);
-          const double e = (64 + ns) * u * Lm * A * fabs(inv_is) + S * dz +
-                           3 * u * ((j + 1) * 1.0) * dL * A * fabs(inv_is) + dk * 2.0 * km * dkap * Lm * fabs(inv_is);
-          worst = fmax(worst, e);
+      const float dkap = __double2float_ru(sqrt(2.0 * dz64 / ((double)km * fmax(1.0 - (double)km, 1e-3))));
+      const float cr = (64 + B.nsamples0) * u;
+      const float gz = dg * (1.0f + km), inv_gz = 1.0f / gz;
+      const float ring = 2.0f * float(PI) * km;
+      // lanes over the table rows, the channels inner: the area at the row's
+      // z is shared by every channel
+      for (int j = lane; j < ng - 1; j += 32) {
+        float kap;
+        const float A0 = ccia_star<float>(km, (float)j * gz, kap);
+        const float rj = 3.0f * u * (float)(j + 1);
+        const float* L = B.ldm + (size_t)pv * B.npb * ng + j;
+        for (int b = 0; b < B.npb; ++b, L += ng) {
+          const float afac = ch[b * TS_CH], dk = fabsf(ch[b * TS_CH + 1]), inv_is = fabsf(ch[b * TS_CH + 2]);
+          if (!isfinite(inv_is)) continue;
+          const float kb = km * sqrtf(afac);
+          const float l0 = L[0], l1 = L[1];
+          const float Lm = fmaxf(fabsf(l0), fabsf(l1)), dL = fabsf(l1 - l0);
+          const float ai = fmaxf(afac * A0, fmaf(dk, ring, A0)) * inv_is;
+          const float S = 2.0f * fminf(fmaxf(kb, km), 1.0f) * Lm * inv_is + ai * dL * inv_gz;
+          const float e = cr * Lm * ai + S * dz + rj * dL * ai + dk * 2.0f * km * dkap * Lm * inv_is;
+          worst = fmaxf(worst, e);
         }
       }
     }
   }
-  for (int off = 16; off > 0; off >>= 1) worst = fmax(worst, __shfl_xor_sync(FULL, worst, off));
+  for (int off = 16; off > 0; off >>= 1) worst = fmaxf(worst, __shfl_xor_sync(FULL, worst, off));
   if (lane == 0) {
-    const double bnd = worst > 0.0 ? worst + u : 0.0;
+    const double bnd = worst > 0.0f ? (double)(worst * BOUND_SAFETY) + BOUND_U : 0.0;
     B.bound[pv] = bnd;
     if (B.bound_max) atomicMax(B.bound_max, (unsigned long long)__double_as_longlong(bnd));
   }

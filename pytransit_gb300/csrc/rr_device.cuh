@@ -506,6 +506,34 @@ __device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
   e = __fmaf_rn(a, b, -p);
 }
 
+// Exact phase-folded time of one point from its FP32-pair time (hi, lo) and
+// the light-curve record (t0 - t_ref pair), starting from the epoch estimate
+// n: tc = (hi + lo) - (d0h + d0l) - n (p_hi + p_lo) with error-free
+// transformations; n is corrected once if the estimate was one off.
+__device__ __forceinline__ float exact_tc_pair(float hi, float lo, float d0h, float d0l, float n, float p_hi,
+                                               float p_lo, float& tail) {
+  float s1, e1, q1, e2, s2, e3;
+  two_sum(hi, -d0h, s1, e1);
+  two_prod(n, p_hi, q1, e2);
+  two_sum(s1, -q1, s2, e3);
+  tail = ((e1 + e3) - e2) + (lo - d0l) - n * p_lo;
+  float t = s2 + tail;
+  if (t >= 0.5f * p_hi || t < -0.5f * p_hi) {
+    n += (t >= 0.5f * p_hi) ? 1.0f : -1.0f;
+    two_prod(n, p_hi, q1, e2);
+    two_sum(s1, -q1, s2, e3);
+    tail = ((e1 + e3) - e2) + (lo - d0l) - n * p_lo;
+  }
+  return s2;   // tc = s2 + tail
+}
+
+__device__ __forceinline__ float exact_tc(float hi, float lo, float d0h, float d0l, float n, float p_hi,
+                                          float p_lo) {
+  float tail;
+  const float s2 = exact_tc_pair(hi, lo, d0h, d0l, n, p_hi, p_lo, tail);
+  return s2 + tail;
+}
+
 // Horner evaluation of the FP32 Taylor coefficients and the separation.
 __device__ __forceinline__ float sep_c_f32(float t, const float* c) {
   float x = fmaf(t, fmaf(t, fmaf(t, fmaf(t, c[4], c[3]), c[2]), c[1]), c[0]);

@@ -142,6 +142,222 @@ es_flux_kernel(const double* __restrict__ times, int npt, const double* __restri
   for (int b = 0; b < npb; ++b) out[(size_t)b * ldflux] /= nsamples0;
 }
 
+// ---------------------------------------------------------------------------
+// Split precision.  The prologue (FP64 eclipse shift, light travel time and
+// Taylor jet, one thread per pv) writes an FP32 record per pv and, per light
+// curve, the box and the eclipse epoch te - t_ref as an FP32 pair in the
+// layout of the transit model's light-curve records (LC_*); the flux kernels
+// walk 128-point tiles as the transit flux kernel does: a tile whose time
+// range reaches no box copy is a run of stores of the out-of-eclipse value,
+// the others fold each point's FP32-pair time exactly (exact_tc) and evaluate
+// the samples of the in-box points in FP32.
+// ---------------------------------------------------------------------------
+constexpr int ECL32 = 16;   // c[0..9], [10] p_hi, [11] p_lo, [12] 1/p_hi, [13] k, [14] flags, [15] pi k^2
+constexpr int ECL_NW = 4;   // warps per block of the split flux kernels
+constexpr int ECL_CHUNK = 32;
+
+struct EclSplitArgs {
+  const float2* times_ff;
+  const int32_t* lcids;
+  int npt, npv, nlc, npb, ldflux;
+  const float *rec, *lcr, *cb;   // [npv][ECL32], [npv][nlc][LC32], ES: [npv][npb] f_b / (pi (1 + f_b k^2))
+  float* flux;
+};
+
+// One pv: FP64 shift, light travel time and jet about mid-eclipse, rounded to
+// FP32; contacts by FP32 bisection on the FP32 coefficients (they only place
+// the box, padded by pad0 + exptime).  For the spectroscopic model (ES),
+// nsamples and exptimes are null and its one record takes ns0 and ex0; the
+// channel factors are written too.
+__global__ void eclipse_prepare_split_kernel(const double* __restrict__ k, const double* __restrict__ t0, int ldt0,
+                                             const double* __restrict__ p, const double* __restrict__ a,
+                                             const double* __restrict__ inc, const double* __restrict__ e,
+                                             const double* __restrict__ w, const double* __restrict__ rstar,
+                                             int npv, int nlc, const int32_t* __restrict__ epids,
+                                             const int32_t* __restrict__ nsamples,
+                                             const double* __restrict__ exptimes, int ns0, double ex0,
+                                             double pad0, double t_ref,
+                                             double t_absmax, const double* __restrict__ fratio, int npb,
+                                             float* __restrict__ rec, float* __restrict__ lcr,
+                                             float* __restrict__ cb) {
+  const int pv = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pv >= npv) return;
+  float* o = rec + (size_t)pv * ECL32;
+  const double kk = k[pv], pp = p[pv];
+  const bool valid = !(isnan(a[pv]) || a[pv] <= 1.0 || e[pv] < 0.0);
+  float cf[10];
+  double shift = 0.0, ltt = 0.0;
+  float t1 = 0.0f, t4 = 0.0f;
+  if (valid) {
+    shift = eclipse_time_offset(pp, e[pv], w[pv]);
+    ltt = eclipse_ltt(a[pv], inc[pv], e[pv], w[pv], rstar[pv]);
+    double c[10];
+    solve2d_phase(shift, pp, a[pv], inc[pv], e[pv], w[pv], c);
+    for (int i = 0; i < 10; ++i) cf[i] = (float)c[i];
+    contact_points14_f32((float)kk, cf, t1, t4);
+  } else {
+    for (int i = 0; i < 10; ++i) cf[i] = 0.0f;
+  }
+  double d0max = 0.0;
+  for (int lc = 0; lc < nlc; ++lc) {
+    const double te = t0[(size_t)pv * ldt0 + (epids ? epids[lc] : 0)] + shift + ltt;
+    d0max = fmax(d0max, fabs(te - t_ref));
+  }
+  const float p_hi = __double2float_rn(pp);
+  // bound of |fast-test tc - true tc|, as for the transit records
+  const double err = ldexp(1.0, -21) * (t_absmax + d0max + pp) + 1e-9;
+  int flags = valid ? FLAG_VALID : 0;
+  for (int lc = 0; lc < nlc; ++lc) {
+    const double ex = exptimes ? exptimes[lc] : ex0;
+    const int ns = nsamples ? nsamples[lc] : ns0;
+    const double te = t0[(size_t)pv * ldt0 + (epids ? epids[lc] : 0)] + shift + ltt;
+    const double d0 = te - t_ref;
+    const double pad = pad0 + ex;
+    const double lo = (double)t1 - pad, hi = (double)t4 + pad;
+    if (hi + 2 * err >= 0.5 * pp || lo - 2 * err <= -0.5 * pp) flags |= FLAG_WIDE;
+    float* q = lcr + ((size_t)pv * nlc + lc) * LC32;
+    const float d0h = __double2float_rn(d0);
+    q[LC_FLO] = (float)(lo - err);
+    q[LC_FHI] = (float)(hi + err);
+    q[LC_D0H] = d0h;
+    q[LC_D0L] = __double2float_rn(d0 - (double)d0h);
+    q[LC_LO] = (float)lo;
+    q[LC_HI] = (float)hi;
+    q[LC_K] = (float)kk;
+    q[LC_INV1PK] = 0.0f;
+    q[LC_INVIS] = 0.0f;
+    q[LC_EXPT] = (float)ex;
+    q[LC_INVNS] = 1.0f / (float)ns;
+    q[LC_NS] = __int_as_float(ns);
+    q[LC_PB] = __int_as_float(0);
+    q[13] = q[14] = q[15] = 0.0f;
+  }
+  for (int i = 0; i < 10; ++i) o[i] = cf[i];
+  o[10] = p_hi;
+  o[11] = __double2float_rn(pp - (double)p_hi);
+  o[12] = 1.0f / p_hi;
+  o[13] = (float)kk;
+  o[14] = __int_as_float(flags);
+  o[15] = (float)(PI * (kk * kk));
+  if (cb)
+    for (int b = 0; b < npb; ++b) {
+      const double f = fratio[(size_t)pv * npb + b];
+      cb[(size_t)pv * npb + b] = (float)(f / (PI * (1.0 + f * (kk * kk))));
+    }
+}
+
+// The in-box value of one point: the mean over its samples of the visible
+// planet area pi k^2 - A(1, k, z) (eclipse model) or the mean occulted area
+// A(1, k, z) (spectroscopic model, which applies the channel factors after).
+template <bool ES>
+__device__ __forceinline__ float ecl_point(const float* orb, const float* R, float tc) {
+  const float k = orb[13], pik2 = orb[15];
+  const int ns = __float_as_int(R[LC_NS]);
+  const float ex = R[LC_EXPT], inv_ns = R[LC_INVNS];
+  float f = 0.0f;
+  for (int s = 0; s < ns; ++s) {
+    const float z = sep_c_f32(tc + ex * fmaf((float)s + 0.5f, inv_ns, -0.5f), orb);
+    float kap;
+    const float ar = ccia_star<float>(k, z, kap);
+    f += ES ? ar : pik2 - ar;
+  }
+  return f * inv_ns;
+}
+
+// The flux kernels: blocks of ECL_NW warps, each block a range of at most
+// `chunk` consecutive 128-point tiles of one pv, the warps over its tiles.
+// Eclipse model: flux[pv, pt] = pi k^2 outside the box, else ecl_point.  ES:
+// flux[pv, b, pt] = 1 outside the box, else 1 - cb[pv, b] * mean area.
+template <bool ES>
+__global__ void __launch_bounds__(ECL_NW * 32) eclipse_flux_split_kernel(EclSplitArgs A, int chunk) {
+  __shared__ __align__(16) float orb[ECL32];
+  extern __shared__ __align__(16) float ecl_smem[];   // LC records [nlc][LC32], then ES channel factors [npb]
+  const int pv = blockIdx.z * 65535 + blockIdx.y;
+  if (pv >= A.npv) return;   // block-uniform
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < ECL32) orb[threadIdx.x] = A.rec[(size_t)pv * ECL32 + threadIdx.x];
+  for (int i = threadIdx.x; i < A.nlc * LC32; i += blockDim.x)
+    ecl_smem[i] = A.lcr[(size_t)pv * A.nlc * LC32 + i];
+  float* cbs = ecl_smem + A.nlc * LC32;
+  if (ES)
+    for (int i = threadIdx.x; i < A.npb; i += blockDim.x) cbs[i] = A.cb[(size_t)pv * A.npb + i];
+  __syncthreads();
+  const float* LCR = ecl_smem;
+  const int flags = __float_as_int(orb[14]);
+  const bool valid = flags & FLAG_VALID, wide = flags & FLAG_WIDE;
+  const float p_hi = orb[10], p_lo = orb[11], inv_p = orb[12];
+  const float outv = !valid ? __int_as_float(0x7fc00000) : (ES ? 1.0f : orb[15]);
+  const int nrow = ES ? A.npb : 1;
+  float* fpv = A.flux + (size_t)pv * nrow * A.ldflux;
+  const bool vec = ((A.ldflux & 3) == 0) && ((reinterpret_cast<uintptr_t>(A.flux) & 15) == 0);
+  const float4 out4 = make_float4(outv, outv, outv, outv);
+  const float4* meta = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(A.times_ff) +
+                                                       time_meta_offset(A.npt));
+  const int ntiles = (A.npt + TIME_TILE - 1) / TIME_TILE;
+  const int tb0 = blockIdx.x * chunk, tb1 = min(ntiles, tb0 + chunk);
+  for (int tile = tb0 + warp; tile < tb1; tile += ECL_NW) {
+    // the tile's cull test, by lane 0 and broadcast: its time range against
+    // the box copies around it (as the transit flux kernel's)
+    bool cull = !valid;
+    if (valid && !wide) {
+      const float4 tm = __ldg(meta + tile);
+      const int tlc = ES ? 0 : __float_as_int(tm.z);   // ES: one record for every point
+      if (tlc >= 0) {
+        const float* R = LCR + tlc * LC32;
+        const float smin = tm.x - R[LC_D0H], smax = tm.y - R[LC_D0H];
+        const float j0f = ceilf((smin - R[LC_FHI]) * inv_p);
+        bool hit = false;
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+          const float jj = j0f + (float)dj;
+          hit = hit || (fmaf(jj, p_hi, R[LC_FLO]) <= smax && fmaf(jj, p_hi, R[LC_FHI]) >= smin);
+        }
+        cull = !hit;
+      }
+    }
+    const int p0 = tile * TIME_TILE;
+    const bool full = p0 + TIME_TILE <= A.npt;
+    if (cull) {
+      for (int b = 0; b < nrow; ++b) {
+        float* row = fpv + (size_t)b * A.ldflux;
+        if (vec && full) {
+          __stcs(reinterpret_cast<float4*>(row + p0) + lane, out4);
+        } else {
+          for (int q = 0; q < 4; ++q)
+            if (p0 + q * 32 + lane < A.npt) __stcs(row + p0 + q * 32 + lane, outv);
+        }
+      }
+      continue;
+    }
+    // slot q of lane l: point p0 + q * 32 + l
+    float val[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int pt = p0 + q * 32 + lane;
+      val[q] = ES ? 0.0f : outv;   // ES: the mean area (0 outside the box)
+      if (pt >= A.npt || !valid) continue;
+      const float2 tt = __ldg(A.times_ff + pt);
+      const float* R = ES ? LCR : LCR + __ldg(A.lcids + pt) * LC32;
+      const float sv = tt.x - R[LC_D0H];
+      const float n = floorf(fmaf(sv, inv_p, 0.5f));
+      const float r = fmaf(-n, p_hi, sv);
+      if (wide || (r >= R[LC_FLO] && r <= R[LC_FHI])) {
+        const float t = exact_tc(tt.x, tt.y, R[LC_D0H], R[LC_D0L], n, p_hi, p_lo);
+        if (R[LC_LO] <= t && t <= R[LC_HI]) val[q] = ecl_point<ES>(orb, R, t);
+      }
+    }
+    for (int b = 0; b < nrow; ++b) {
+      float* row = fpv + (size_t)b * A.ldflux;
+      const float c = ES ? cbs[b] : 0.0f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int pt = p0 + q * 32 + lane;
+        if (pt < A.npt) __stcs(row + pt, ES ? (valid ? 1.0f - c * val[q] : outv) : val[q]);
+      }
+    }
+  }
+}
+
 }  // namespace rr
 
 using namespace rr;
@@ -180,6 +396,71 @@ int rr_es_f64(const double* times, int npt, const double* k, const double* t0, c
   dim3 fg((npt + 255) / 256, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
   es_flux_kernel<<<fg, 256, 0, s>>>(times, npt, k, t0, p, fratio, npb, nsamples0, exptime0, rec, npv, flux, ldflux);
   return check_launch("rr_es_f64");
+}
+
+size_t rr_eclipse_split_workspace_bytes(int npv, int nlc, int npb) {
+  const size_t n = (size_t)(npv > 0 ? npv : 1);
+  return sizeof(float) * n * (ECL32 + (size_t)(nlc > 0 ? nlc : 1) * LC32 + (size_t)(npb > 0 ? npb : 1)) + 3 * 256;
+}
+
+static int eclipse_split_launch(bool es, const float* times_ff, double t_ref, double t_absmax, int npt,
+                                const double* k, const double* t0, int ldt0, const double* p, const double* a,
+                                const double* inc, const double* e, const double* w, const double* rstar,
+                                const double* fratio, int npv, int nlc, int npb, const int32_t* lcids,
+                                const int32_t* epids, const int32_t* nsamples, const double* exptimes,
+                                int ns0, double ex0, double pad0, void* workspace, size_t workspace_bytes, float* flux, int ldflux,
+                                void* stream, const char* name) {
+  if (workspace_bytes < rr_eclipse_split_workspace_bytes(npv, nlc, npb)) return RR_ERR_WORKSPACE;
+  const size_t smem = sizeof(float) * ((size_t)nlc * LC32 + (es ? (size_t)npb : 0));
+  if (smem > 48 * 1024) return RR_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  Carve cv(workspace);
+  float* rec = cv.take<float>((size_t)npv * ECL32);
+  float* lcr = cv.take<float>((size_t)npv * nlc * LC32);
+  float* cb = es ? cv.take<float>((size_t)npv * npb) : nullptr;
+  // one warp per block: the FP64 chains spread over every SM
+  eclipse_prepare_split_kernel<<<(npv + 31) / 32, 32, 0, s>>>(k, t0, ldt0, p, a, inc, e, w, rstar, npv, nlc, epids,
+                                                              nsamples, exptimes, ns0, ex0, pad0, t_ref,
+                                                              t_absmax, fratio,
+                                                              npb, rec, lcr, cb);
+  EclSplitArgs A{};
+  A.times_ff = reinterpret_cast<const float2*>(times_ff);
+  A.lcids = lcids;
+  A.npt = npt; A.npv = npv; A.nlc = nlc; A.npb = npb; A.ldflux = ldflux;
+  A.rec = rec; A.lcr = lcr; A.cb = cb; A.flux = flux;
+  const int ntiles = (npt + TIME_TILE - 1) / TIME_TILE;
+  long long chunk = (long long)ntiles * npv / (4LL * sm_count() * ECL_NW * 8);
+  chunk = chunk < ECL_NW ? ECL_NW : (chunk > ECL_CHUNK ? ECL_CHUNK : chunk);
+  dim3 g((unsigned)((ntiles + chunk - 1) / chunk), npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
+  if (es)
+    eclipse_flux_split_kernel<true><<<g, ECL_NW * 32, smem, s>>>(A, (int)chunk);
+  else
+    eclipse_flux_split_kernel<false><<<g, ECL_NW * 32, smem, s>>>(A, (int)chunk);
+  return check_launch(name);
+}
+
+int rr_eclipse_split(const float* times_ff, double t_ref, double t_absmax, int npt, const double* k,
+                     const double* t0, int ldt0, const double* p, const double* a, const double* inc,
+                     const double* e, const double* w, const double* rstar, int npv, int nlc, const int32_t* lcids,
+                     const int32_t* epids, const int32_t* nsamples, const double* exptimes, void* workspace,
+                     size_t workspace_bytes, float* flux, int ldflux, void* stream) {
+  if (npt < 0 || npv < 0 || nlc < 1 || ldt0 < 1 || ldflux < npt) return RR_ERR_ARG;
+  if (npv == 0 || npt == 0) return RR_OK;
+  return eclipse_split_launch(false, times_ff, t_ref, t_absmax, npt, k, t0, ldt0, p, a, inc, e, w, rstar, nullptr,
+                              npv, nlc, 1, lcids, epids, nsamples, exptimes, 0, 0.0, 0.003, workspace,
+                              workspace_bytes,
+                              flux, ldflux, stream, "rr_eclipse_split");
+}
+
+int rr_es_split(const float* times_ff, double t_ref, double t_absmax, int npt, const double* k,
+                const double* t0, const double* p, const double* a, const double* inc, const double* e,
+                const double* w, const double* rstar, const double* fratio, int npv, int npb, int nsamples0,
+                double exptime0, void* workspace, size_t workspace_bytes, float* flux, int ldflux, void* stream) {
+  if (npt < 0 || npv < 0 || npb < 1 || nsamples0 < 1 || ldflux < npt) return RR_ERR_ARG;
+  if (npv == 0 || npt == 0) return RR_OK;
+  return eclipse_split_launch(true, times_ff, t_ref, t_absmax, npt, k, t0, 1, p, a, inc, e, w, rstar, fratio, npv,
+                              1, npb, nullptr, nullptr, nullptr, nullptr, nsamples0, exptime0, 0.0015, workspace,
+                              workspace_bytes, flux, ldflux, stream, "rr_es_split");
 }
 
 }  // extern "C"

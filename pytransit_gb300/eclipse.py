@@ -8,8 +8,12 @@ eclipse models.
   (pytransit/models/roadrunner/esmodel.py:29-92): npb flux ratios sharing one
   orbit (esmodel, model_ecspec.py:13-63).
 
-Both run as FP64 CUDA kernels (rr_eclipse_f64, rr_es_f64) on the RoadRunner
-orbit layer expanded about mid-eclipse.  One deliberate difference: the
+Both run on the RoadRunner orbit layer expanded about mid-eclipse, as FP64
+CUDA kernels (rr_eclipse_f64, rr_es_f64; precision='fp64', the default) or in
+split precision (rr_eclipse_split, rr_es_split; precision='split'): FP64
+per-pv prologue, exact FP32-pair phase fold, FP32 per-sample areas and FP32
+output, with the 128-point tiles outside every eclipse window written as
+plain runs of the out-of-eclipse value.  One deliberate difference: the
 reference's EclipseModel.evaluate passes the passband indices where the
 kernel expects the epoch indices (new_eclipse_model.py:66); here the epoch
 indices of set_data are used.
@@ -32,6 +36,11 @@ _SIG = {
                         _vp, _i, _vp], _i),
     'rr_es_f64': ([_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp, _sz, _vp, _i, _vp],
                   _i),
+    'rr_eclipse_split_workspace_bytes': ([_i, _i, _i], _sz),
+    'rr_eclipse_split': ([_vp, _d, _d, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp,
+                          _vp, _sz, _vp, _i, _vp], _i),
+    'rr_es_split': ([_vp, _d, _d, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp, _sz, _vp, _i,
+                     _vp], _i),
 }
 _lib._EXTRA_SIGNATURES.update(_SIG)
 
@@ -54,17 +63,15 @@ def _vec(x, npv, name):
 
 
 class _GpuEclipseBase(TransitModel):
-    def __init__(self, device=None):
+    def __init__(self, precision: str = 'fp64', device=None):
         super().__init__()
+        if precision not in ('fp64', 'split'):
+            raise ValueError("precision must be 'fp64' or 'split'")
+        self.precision = precision
         self.device = device
 
     def _cuda_device(self):
         return _lib.require_cuda(self.device)
-
-    @staticmethod
-    def _to(dev, **arrays):
-        import torch
-        return {n: torch.as_tensor(np.ascontiguousarray(v)).to(dev) for n, v in arrays.items()}
 
 
 class EclipseModel(_GpuEclipseBase):
@@ -85,19 +92,29 @@ class EclipseModel(_GpuEclipseBase):
         vecs = {n: _vec(x, npv, n) for n, x in (('p', p), ('a', a), ('i', i), ('e', 0.0 if e is None else e),
                                                 ('w', 0.0 if w is None else w), ('rstar', rstar))}
         dd = self._device_data(dev)
-        g = self._to(dev, k=k, t0=t0, **vecs)
+        g = self._upload(dict(k=k, t0=t0, **vecs), dev)   # one pinned host-to-device copy
         L = _L()
         P = _lib.ptr
-        wsb = L.rr_eclipse_workspace_bytes(npv)
-        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
-        out = torch.empty((npv, self.npt), dtype=torch.float64, device=dev)
-        _lib.check(L.rr_eclipse_f64(P(dd['time']), self.npt, P(g['k']), P(g['t0']), t0.shape[1], P(g['p']), P(g['a']),
-                                    P(g['i']), P(g['e']), P(g['w']), P(g['rstar']), npv, self.nlc, P(dd['lcids']),
-                                    P(dd['epids']), P(dd['nsamples']), P(dd['exptimes']), P(ws), wsb, P(out),
-                                    self.npt, _lib.stream_ptr(dev)), "rr_eclipse_f64")
+        if self.precision == 'split':
+            wsb = L.rr_eclipse_split_workspace_bytes(npv, self.nlc, 1)
+            ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+            out = torch.empty((npv, self.npt), dtype=torch.float32, device=dev)
+            _lib.check(L.rr_eclipse_split(P(dd['times_ff']), dd['t_ref'], dd['t_absmax'], self.npt, P(g['k']),
+                                          P(g['t0']), t0.shape[1], P(g['p']), P(g['a']), P(g['i']), P(g['e']),
+                                          P(g['w']), P(g['rstar']), npv, self.nlc, P(dd['lcids']), P(dd['epids']),
+                                          P(dd['nsamples']), P(dd['exptimes']), P(ws), wsb, P(out), self.npt,
+                                          _lib.stream_ptr(dev)), "rr_eclipse_split")
+        else:
+            wsb = L.rr_eclipse_workspace_bytes(npv)
+            ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+            out = torch.empty((npv, self.npt), dtype=torch.float64, device=dev)
+            _lib.check(L.rr_eclipse_f64(P(dd['time']), self.npt, P(g['k']), P(g['t0']), t0.shape[1], P(g['p']),
+                                        P(g['a']), P(g['i']), P(g['e']), P(g['w']), P(g['rstar']), npv, self.nlc,
+                                        P(dd['lcids']), P(dd['epids']), P(dd['nsamples']), P(dd['exptimes']), P(ws),
+                                        wsb, P(out), self.npt, _lib.stream_ptr(dev)), "rr_eclipse_f64")
         if not copy:
             return out
-        return np.squeeze(out.cpu().numpy())
+        return np.squeeze(out.cpu().numpy().astype(np.float64, copy=False))
 
     def __call__(self, *args, **kwargs):
         return self.evaluate(*args, **kwargs)
@@ -105,6 +122,10 @@ class EclipseModel(_GpuEclipseBase):
 
 class EclipseSpectroscopyModel(_GpuEclipseBase):
     """Secondary eclipse for npb channels (flux ratios f[npv, npb]) sharing one orbit."""
+
+    def __init__(self, parallel: bool = False, precision: str = 'fp64', device=None):
+        # the reference's ``parallel`` selects its numba variant; one GPU path here
+        super().__init__(precision=precision, device=device)
 
     def evaluate(self, f, k, t0, p, a, i, e=0.0, w=0.0, rstar: Union[float, ndarray] = 1.0, copy: bool = True):
         """flux[npv, npb, npt] (numpy with copy=True, else the CUDA tensor);
@@ -122,18 +143,27 @@ class EclipseSpectroscopyModel(_GpuEclipseBase):
         vecs = {n: _vec(x, npv, n) for n, x in (('t0', t0), ('p', p), ('a', a), ('i', i), ('e', e), ('w', w),
                                                 ('rstar', rstar))}
         dd = self._device_data(dev)
-        g = self._to(dev, k=k, f=f, **vecs)
+        g = self._upload(dict(k=k, f=f, **vecs), dev)
         L = _L()
         P = _lib.ptr
-        wsb = L.rr_eclipse_workspace_bytes(npv)
-        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
-        out = torch.empty((npv, npb, self.npt), dtype=torch.float64, device=dev)
         ns0 = int(np.atleast_1d(self.nsamples)[0])
         ex0 = float(np.atleast_1d(self.exptimes)[0])
-        _lib.check(L.rr_es_f64(P(dd['time']), self.npt, P(g['k']), P(g['t0']), P(g['p']), P(g['a']), P(g['i']),
-                               P(g['e']), P(g['w']), P(g['rstar']), P(g['f']), npv, npb, ns0, ex0, P(ws), wsb, P(out),
-                               self.npt, _lib.stream_ptr(dev)), "rr_es_f64")
-        return out.cpu().numpy() if copy else out
+        if self.precision == 'split':
+            wsb = L.rr_eclipse_split_workspace_bytes(npv, 1, npb)
+            ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+            out = torch.empty((npv, npb, self.npt), dtype=torch.float32, device=dev)
+            _lib.check(L.rr_es_split(P(dd['times_ff']), dd['t_ref'], dd['t_absmax'], self.npt, P(g['k']), P(g['t0']),
+                                     P(g['p']), P(g['a']), P(g['i']), P(g['e']), P(g['w']), P(g['rstar']), P(g['f']),
+                                     npv, npb, ns0, ex0, P(ws), wsb, P(out), self.npt, _lib.stream_ptr(dev)),
+                       "rr_es_split")
+        else:
+            wsb = L.rr_eclipse_workspace_bytes(npv)
+            ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+            out = torch.empty((npv, npb, self.npt), dtype=torch.float64, device=dev)
+            _lib.check(L.rr_es_f64(P(dd['time']), self.npt, P(g['k']), P(g['t0']), P(g['p']), P(g['a']), P(g['i']),
+                                   P(g['e']), P(g['w']), P(g['rstar']), P(g['f']), npv, npb, ns0, ex0, P(ws), wsb,
+                                   P(out), self.npt, _lib.stream_ptr(dev)), "rr_es_f64")
+        return out.cpu().numpy().astype(np.float64, copy=False) if copy else out
 
     def __call__(self, *args, **kwargs):
         return self.evaluate(*args, **kwargs)

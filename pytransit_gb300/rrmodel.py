@@ -299,34 +299,6 @@ class RoadRunnerModel(TransitModel):
         istar_d = torch.as_tensor(np.array(istar, dtype=np.float64)).to(device=device, dtype=dt)
         return ldp_d, istar_d
 
-    def _upload(self, arrays, device):
-        """Send the small per-call arrays in one host-to-device copy through a
-        reused pinned staging buffer; returns device views of the same shapes."""
-        import torch
-        names = [n for n, v in arrays.items() if v is not None]
-        sizes = [int(arrays[n].size) for n in names]
-        total = sum(sizes)
-        if getattr(self, '_pin', None) is None or self._pin.numel() < total or self._pin_dev.device != device:
-            n = max(total, 1024)
-            self._pin = torch.empty(n, dtype=torch.float64, pin_memory=True)
-            self._pin_dev = torch.empty(n, dtype=torch.float64, device=device)
-            self._pin_evt = None
-        if self._pin_evt is not None:
-            self._pin_evt.synchronize()      # the previous copy has left the staging buffer
-        hp = self._pin.numpy()
-        off = 0
-        for n, sz in zip(names, sizes):
-            hp[off:off + sz] = np.asarray(arrays[n], dtype=np.float64).reshape(-1)
-            off += sz
-        self._pin_dev[:total].copy_(self._pin[:total], non_blocking=True)
-        self._pin_evt = torch.cuda.Event()
-        self._pin_evt.record()
-        out, off = {}, 0
-        for n, sz in zip(names, sizes):
-            out[n] = self._pin_dev[off:off + sz].view(arrays[n].shape)
-            off += sz
-        return out
-
     # ------------------------------------------------------------------
     def _flux_to_host(self, dd, npt, npv, nlc, npb, ws, out2d, device, nchunks=8):
         """Split-path flux into the pinned host rows out2d[npv, npt]: the pv

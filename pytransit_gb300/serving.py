@@ -54,6 +54,18 @@ SERVE_REQUEST_DTYPE = np.dtype([('times_ff', 'u8'), ('lcids', 'u8'), ('orb32', '
                                 ('dg', 'f8'), ('nsamples0', 'i4'), ('pad', 'i4')])
 
 
+# rr_serve_setup_args (include/pytransit_gb300.h), field by field, all 8 bytes
+SETUP_ARGS_DTYPE = np.dtype(
+    [(n, 'u8') for n in ('stage', 'dst')] + [('n_in', 'i8')] +
+    [(n, 'u8') for n in ('time', 'lcids', 'pbids', 'epids', 'nsamples', 'exptimes', 'k', 't0', 'p', 'a', 'inc', 'e',
+                         'w', 'ldc', 'times_ff', 'ldp', 'istar', 'ws', 'bnd', 'bmax', 'flux', 'mu', 'basis',
+                         'weights', 'z_edges')] +
+    [(n, 'i8') for n in ('npt', 'npv', 'nlc', 'npb', 'nep', 'nkc', 'npar', 'law', 'nb', 'nk', 'nz', 'ng', 'ldflux',
+                         'wsb', 'nsamples0')] +
+    [(n, 'f8') for n in ('t_ref', 't_abs', 'dk', 'kmin', 'kmax', 'dg', 'exptime0')] +
+    [(n, 'u8') for n in ('bound_host', 'desc')])
+
+
 @dataclass
 class Request:
     """One evaluation.  kind 'rr' (flux[npv, npt]) or 'ts' (flux[npv, npb, npt]).
@@ -86,7 +98,10 @@ class ServerStats:
     than the budget or the arena); ``failed``: requests whose set-up, launch or
     copy raised; ``cancelled``: futures the caller cancelled while queued;
     ``bypassed``: admissions that passed a blocked request at the head of the
-    queue."""
+    queue.  Time of the scheduler thread (seconds): ``admit_s`` in admission
+    and per-request set-up, ``step_s`` in issuing steps, ``poll_s`` in
+    completions; ``gpu_step_s``: device time of the finished batched steps
+    (CUDA events around each step's kernel)."""
     submitted: int = 0
     admitted: int = 0
     completed: int = 0
@@ -98,6 +113,10 @@ class ServerStats:
     points: int = 0
     peak_bytes: int = 0
     max_queue: int = 0
+    admit_s: float = 0.0
+    step_s: float = 0.0
+    poll_s: float = 0.0
+    gpu_step_s: float = 0.0
     latencies: list = field(default_factory=list)
     done_times: list = field(default_factory=list)
 
@@ -106,7 +125,8 @@ class ServerStats:
         return dict(submitted=self.submitted, admitted=self.admitted, completed=self.completed,
                     rejected=self.rejected, failed=self.failed, cancelled=self.cancelled, bypassed=self.bypassed,
                     steps=self.steps, points=self.points, peak_hbm_bytes=self.peak_bytes,
-                    max_queue=self.max_queue, p50_s=float(np.percentile(lat, 50)),
+                    max_queue=self.max_queue, admit_s=self.admit_s, step_s=self.step_s, poll_s=self.poll_s,
+                    gpu_step_s=self.gpu_step_s, p50_s=float(np.percentile(lat, 50)),
                     p99_s=float(np.percentile(lat, 99)), mean_s=float(lat.mean()))
 
 
@@ -247,29 +267,54 @@ class _PinnedRing:
         self.live.append((lo, lo + ((n + 255) & ~255), event))
 
 
-def ts_work_items(npv: int, npt: int, tiles: int = TS_ITEM_TILES) -> np.ndarray:
-    """Rows (pv, pv + 1, tile0, tile1) of at most `tiles` tiles each (int32),
-    for a transmission-spectroscopy request: every tile writes all its
-    channel rows, so an item is one pv and a short tile range."""
-    ntiles = max(1, (npt + TILE - 1) // TILE)
-    t0 = np.arange(0, ntiles, tiles)
-    pv = np.repeat(np.arange(npv), t0.size)
-    tt = np.tile(t0, npv)
-    return np.stack([pv, pv + 1, tt, np.minimum(tt + tiles, ntiles)], 1).astype(np.int32)
+class WorkItems:
+    """The work items of one request, rows (pv0, pv1, tile0, tile1) (int32),
+    computed for the slice a step takes rather than kept per request: a large
+    request has hundreds of thousands of items.  Either every item is one pv
+    and a range of `per` tiles (`by_tiles`), or a range of `per` pvs over all
+    tiles."""
+
+    def __init__(self, npv: int, ntiles: int, per: int, by_tiles: bool):
+        self.npv, self.ntiles, self.per, self.by_tiles = npv, ntiles, per, by_tiles
+        self.nt = -(-ntiles // per) if by_tiles else 1           # items per pv
+        self.n = npv * self.nt if by_tiles else -(-npv // per)
+        # a short list is cheaper kept whole than computed slice by slice
+        self._rows = self._make(slice(None)) if self.n <= 4096 else None
+
+    def __len__(self):
+        return self.n
+
+    def __getitem__(self, sl):
+        return self._rows[sl] if self._rows is not None else self._make(sl)
+
+    def _make(self, sl):
+        i = np.arange(*sl.indices(self.n), dtype=np.int64)
+        if self.by_tiles:
+            pv = i // self.nt
+            t0 = (i % self.nt) * self.per
+            rows = (pv, pv + 1, t0, np.minimum(t0 + self.per, self.ntiles))
+        else:
+            pv0 = i * self.per
+            rows = (pv0, np.minimum(pv0 + self.per, self.npv), np.zeros_like(i), np.full_like(i, self.ntiles))
+        return np.stack(rows, 1).astype(np.int32)
+
+    def __iter__(self):
+        return iter(self[:])
 
 
-def work_items(npv: int, npt: int, target_tiles: int = 256) -> np.ndarray:
-    """Rows (pv0, pv1, tile0, tile1) of about target_tiles pv-tiles each (int32)."""
+def ts_work_items(npv: int, npt: int, tiles: int = TS_ITEM_TILES) -> WorkItems:
+    """Items (pv, pv + 1, tile0, tile1) of at most `tiles` tiles each, for a
+    transmission-spectroscopy request: every tile writes all its channel
+    rows, so an item is one pv and a short tile range."""
+    return WorkItems(npv, max(1, (npt + TILE - 1) // TILE), tiles, True)
+
+
+def work_items(npv: int, npt: int, target_tiles: int = 256) -> WorkItems:
+    """Items (pv0, pv1, tile0, tile1) of about target_tiles pv-tiles each."""
     ntiles = max(1, (npt + TILE - 1) // TILE)
     if ntiles >= target_tiles:
-        t0 = np.arange(0, ntiles, target_tiles)
-        pv = np.repeat(np.arange(npv), t0.size)
-        tt = np.tile(t0, npv)
-        return np.stack([pv, pv + 1, tt, np.minimum(tt + target_tiles, ntiles)], 1).astype(np.int32)
-    per = max(1, target_tiles // ntiles)
-    pv0 = np.arange(0, npv, per)
-    return np.stack([pv0, np.minimum(pv0 + per, npv), np.zeros_like(pv0), np.full_like(pv0, ntiles)],
-                    1).astype(np.int32)
+        return WorkItems(npv, ntiles, target_tiles, True)
+    return WorkItems(npv, ntiles, max(1, target_tiles // ntiles), False)
 
 
 class RRServer:
@@ -510,7 +555,10 @@ class RRServer:
                     self._cv.wait(timeout=0.01)
                     continue
             try:
+                t0 = time.perf_counter()
                 self._admit()
+                t1 = time.perf_counter()
+                self.stats.admit_s += t1 - t0
                 batch = self._take_items()
                 ts_work, self._ts_new = self._ts_new, []
                 if batch or ts_work:
@@ -526,6 +574,8 @@ class RRServer:
                     for r in {id(r): r for r, _ in batch}.values():
                         if r.state['icur'] >= len(r.state['items']):
                             self._issued[r.rid] = r
+                t2 = time.perf_counter()
+                self.stats.step_s += t2 - t1
                 # completions, polled in issue order: stop at the few oldest still running
                 pending = 0
                 for r in list(self._issued.values()):
@@ -543,6 +593,10 @@ class RRServer:
                         pending += 1
                         if pending >= 4:
                             break
+                steps_done = getattr(self.ex, 'finished_step_seconds', None)
+                if steps_done is not None:
+                    self.stats.gpu_step_s = steps_done()
+                self.stats.poll_s += time.perf_counter() - t2
             except Exception as exc:
                 # a fault of the scheduler itself: every request it holds fails
                 # rather than waiting forever; queued requests are served after
@@ -586,6 +640,8 @@ class GpuExecutor:
         self.setup_stream = torch.cuda.Stream(self.device)    # per-request uploads and prologues
         self.copy_stream = torch.cuda.Stream(self.device)
         self.ts_streams = [torch.cuda.Stream(self.device) for _ in range(4)]
+        self._step_events = collections.deque()   # (start, end) of issued batched steps
+        self._step_seconds = 0.0
         self._ts_next = 0
         self._sp_setup = self.setup_stream.cuda_stream
         self.ring = _PinnedRing(torch, 256 << 20)
@@ -617,6 +673,19 @@ class GpuExecutor:
         # per slot: the stated error bound of the request holding it
         self.bound_pin = torch.zeros(self.MAX_REQ, dtype=torch.float64, pin_memory=True)
         self.bound_np = self.bound_pin.numpy()
+        # the argument record of rr_serve_setup, refilled for every request
+        self.L.rr_serve_setup.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+        self.L.rr_serve_setup_args_size.argtypes = [C.POINTER(C.c_int)]
+        self.L.rr_serve_setup_args_size.restype = None
+        sz = C.c_int()
+        self.L.rr_serve_setup_args_size(C.byref(sz))
+        if sz.value != SETUP_ARGS_DTYPE.itemsize:
+            raise RuntimeError("rr_serve_setup_args layout mismatch with the library")
+        self._setup_rec = np.zeros(1, SETUP_ARGS_DTYPE)
+        self._setup_ptr = self._setup_rec.ctypes.data
+        self._ring_base = self.ring.buf.data_ptr()
+        self._bound_base = self.bound_pin.data_ptr()
+        self._desc_base = self.descs_pin.data_ptr()
         self.graph = None
         self._capture()
 
@@ -710,79 +779,45 @@ class GpuExecutor:
         tmin, tmax = float(h['time'].min()), float(h['time'].max())
         t_ref = 0.5 * (tmin + tmax)
         t_abs = max(tmax - t_ref, t_ref - tmin)
-        sp = self._sp_setup
-        with torch.cuda.stream(self.setup_stream):
-            buf = self.arena.buf[blk:blk + total]
-            base = self.arena.base + blk
-            P = {name: base + o for name, o in off.items()}
-            if own_flux:
+        base = self.arena.base + blk
+        P = {name: base + o for name, o in off.items()}
+        fl = None
+        if own_flux:
+            with torch.cuda.stream(self.setup_stream):
                 fl = torch.empty(flux_bytes // 4, dtype=torch.float32, device=self.device)
-                P['flux'] = fl.data_ptr()
-            buf[:n_in].copy_(stage[lo:lo + n_in], non_blocking=True)
-            self._lib.check(L.rr_time_split(P['time'], P['lcids'], npt, t_ref, P['times_ff'], sp))
-            g = dict(P=P, t_ref=t_ref, t_abs=t_abs, wsb=wsb, block=(blk, total))
-            if req.kind == 'rr':
-                # LD tables, LD means and orbit records in one launch
+            P['flux'] = fl.data_ptr()
+        g = dict(P=P, t_ref=t_ref, t_abs=t_abs, wsb=wsb, block=(blk, total))
+        slot = self.free_slots.pop()
+        req.state['slot'] = slot
+        kind = 0 if req.kind == 'rr' else 1
+        with_desc = kind == 0 or req.state['persistent']
+        if with_desc:
+            # the flux as a tensor is made only when a result is handed over
+            shape = (npv, ldf) if kind == 0 else (npv, npb, ldf)
+            g['flux_src'] = (fl, blk + off.get('flux', 0), shape)
+            self._dirty.add(slot)
+        else:
+            g['chunk'] = chunk
+        basis = None
+        if kind == 0:
+            if ('basis', npar) in tb:
                 basis, nb = m._basis(self.device, npar, True)
-                self._lib.check(L.rr_prepare_split_ld(
-                    t_ref, t_abs, P['k'], h['k'].shape[1], P['t0'], nep, nep, P['p'], P['a'], P['i'], P['e'],
-                    P['w'], npv, nlc, npb, P['pbids'], P['epids'], P['nsamples'], P['exptimes'], m.ld_law,
-                    P['ldc'], npar, tb['mu_ptr'], nz, None if basis is None else basis.data_ptr(), nb,
-                    tb['W32_ptr'], m.nk, ng, m.dk, m.klims[0], m.klims[1], tb['ze_ptr'], P['ldp'], P['istar'],
-                    P['ws'], wsb, sp))
-                g['flux'] = (fl if own_flux else buf[off['flux']:off['flux'] + 4 * npv * ldf].view(torch.float32)
-                             ).view(npv, ldf)
-                orb, lc, ldm = C.c_void_p(), C.c_void_p(), C.c_void_p()
-                L.rr_full_split_tables(P['ws'], npv, npb, nlc, nep, ng, C.byref(orb), C.byref(lc), C.byref(ldm))
-                slot = self.free_slots.pop()
-                req.state['slot'] = slot
-                d = self.descs_h[slot]
-                d['times_ff'], d['lcids'] = P['times_ff'], P['lcids']
-                d['orb32'], d['lc32'], d['ldm'] = orb.value, lc.value, ldm.value
-                d['flux'], d['ldflux'] = P['flux'], ldf
-                d['npt'], d['npv'], d['nlc'], d['npb'], d['ng'] = npt, npv, nlc, npb, ng
-                d['kind'], d['nsamples0'], d['exptime0'] = 0, 0, 0.0
-                d['dg'], d['inv_dg'] = m.dg, np.float32(1.0 / m.dg)
-                self._dirty.add(slot)
             else:
-                # LD profiles, integrals, orbit records and LD means in one launch
-                self._lib.check(L.rr_ts_prepare_split_ld(
-                    m.ld_law, P['ldc'], npar, tb['mu_ptr'], t_ref, t_abs, P['k'], P['t0'], P['p'], P['a'], P['i'],
-                    P['e'], P['w'], npv, npb, float(h['exptimes'][0]), ng, nz, tb['ze_ptr'], P['ws'], wsb, sp),
-                    "rr_ts_prepare_split_ld")
-                g['chunk'] = chunk
-                if req.state['persistent']:
-                    n = 4 * npv * npb * ldf
-                    g['flux'] = (fl if own_flux else buf[off['flux']:off['flux'] + n].view(torch.float32)
-                                 ).view(npv, npb, ldf)
-                    orb, ch, ldm = C.c_void_p(), C.c_void_p(), C.c_void_p()
-                    L.rr_ts_tables(P['ws'], 1, npv, npb, ng, C.byref(orb), C.byref(ch), C.byref(ldm))
-                    slot = self.free_slots.pop()
-                    req.state['slot'] = slot
-                    d = self.descs_h[slot]
-                    d['times_ff'], d['lcids'] = P['times_ff'], 0
-                    d['orb32'], d['lc32'], d['ldm'] = orb.value, ch.value, ldm.value
-                    d['flux'], d['ldflux'] = g['flux'].data_ptr(), ldf
-                    d['npt'], d['npv'], d['nlc'], d['npb'], d['ng'] = npt, npv, 1, npb, ng
-                    d['kind'], d['nsamples0'] = 1, int(h['nsamples'][0])
-                    d['exptime0'] = np.float32(h['exptimes'][0])
-                    d['dg'], d['inv_dg'] = m.dg, np.float32(1.0 / m.dg)
-                    self._dirty.add(slot)
-            # the request's stated error bound (largest over its parameter
-            # vectors), copied to its host slot behind the set-up
-            if 'slot' not in req.state:
-                req.state['slot'] = self.free_slots.pop()
-            bslot = req.state['slot']
-            prm = [P[n] for n in ('p', 'a', 'i', 'e', 'w')]
-            if req.kind == 'rr':
-                rc = L.rr_split_error_bounds(*prm, npv, npb, nlc, h['t0'].shape[1], ng, m.dg, P['ws'], P['bnd'],
-                                             P['bmax'], sp)
-            else:
-                rc = L.rr_ts_split_error_bounds(*prm, npv, npb, ng, m.dg, int(h['nsamples'][0]),
-                                                float(h['exptimes'][0]), P['ws'], P['bnd'], P['bmax'], sp)
-            self._lib.check(rc, "rr_error_bounds")
-            self.bound_pin[bslot:bslot + 1].copy_(buf[off['bmax']:off['bmax'] + 8].view(torch.float64),
-                                                  non_blocking=True)
+                with torch.cuda.stream(self.setup_stream):   # built once, ordered before the prologues
+                    basis, nb = m._basis(self.device, npar, True)
+        # one native call: inputs to the device, time split, fused prologue,
+        # descriptor, error bound (setup_args_dtype mirrors rr_serve_setup_args)
+        self._setup_rec[0] = (
+            self._ring_base + lo if stage is self.ring.buf else stage.data_ptr() + lo, base, n_in,
+            P['time'], P['lcids'], P['pbids'], P['epids'], P['nsamples'], P['exptimes'], P['k'], P['t0'], P['p'],
+            P['a'], P['i'], P['e'], P['w'], P['ldc'], P['times_ff'], P.get('ldp', 0), P.get('istar', 0), P['ws'],
+            P['bnd'], P['bmax'], P.get('flux', 0), tb['mu_ptr'], 0 if basis is None else basis.data_ptr(),
+            tb['W32_ptr'], tb['ze_ptr'],
+            npt, npv, nlc, npb, h['t0'].shape[1] if h['t0'].ndim > 1 else 1, h['k'].shape[1], npar, m.ld_law, nb if kind == 0 else 0, m.nk,
+            nz, ng, ldf, wsb, int(h['nsamples'][0]),
+            t_ref, t_abs, m.dk, m.klims[0], m.klims[1], m.dg, float(h['exptimes'][0]),
+            self._bound_base + 8 * slot, self._desc_base + self.desc_dtype.itemsize * slot if with_desc else 0)
+        self._lib.check(L.rr_serve_setup(kind, self._setup_ptr, self._sp_setup), "rr_serve_setup")
         ready = torch.cuda.Event()
         ready.record(self.setup_stream)
         if stage is self.ring.buf:
@@ -792,6 +827,15 @@ class GpuExecutor:
         g['ready'] = ready
         req.state['g'] = g
         req.state['model'] = m
+
+    def _flux_view(self, req):
+        """The request's flux [npv, (npb,) npt] as a tensor view."""
+        fl, o, shape = req.state['g']['flux_src']
+        if fl is None:
+            n = int(np.prod(shape))
+            fl = self.arena.buf[o:o + 4 * n].view(self.torch.float32)
+        res = fl.view(shape)
+        return res[..., :req.npt]
 
     # -- steps -------------------------------------------------------------------
     def step(self, batch, ts_reqs):
@@ -831,9 +875,15 @@ class GpuExecutor:
                 cev = torch.cuda.Event()
                 cev.record(self.stream)
                 self.ring.commit(lo, nb, cev)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e0.record(self.stream)
                 self.graph.replay()
-            ev = torch.cuda.Event()
-            ev.record(self.stream)
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record(self.stream)
+                self._step_events.append((e0, ev))
+            else:
+                ev = torch.cuda.Event()
+                ev.record(self.stream)
             for r, _ in batch:
                 r.state['last_event'] = ev
         # transmission-spectroscopy requests run as their own launches on a
@@ -894,12 +944,11 @@ class GpuExecutor:
         if req.kind == 'ts' and not req.state.get('persistent'):
             req.state['copy_event'] = req.state['ts_done_event']
             return
-        g = req.state['g']
-        res = g['flux'][:, :req.npt] if req.kind == 'rr' else g['flux'][:, :, :req.npt]
         if self.result == 'device':
-            req.state['host_out'] = res
+            req.state['host_out'] = self._flux_view(req) if req.state.get('keep', True) else None
             req.state['copy_event'] = req.state['last_event']
             return
+        res = self._flux_view(req)
         host = torch.empty(tuple(res.shape), dtype=torch.float32, pin_memory=True)
         self.copy_stream.wait_event(req.state['last_event'])
         with torch.cuda.stream(self.copy_stream):
@@ -916,6 +965,8 @@ class GpuExecutor:
         req.state['copy_done'] = True
         req.state['error_bound'] = float(self.bound_np[req.state['slot']])
         out = req.state['host_out']
+        if out is None:          # a dropped result (keep_result=False): its point count stands for it
+            return req.points
         return out if self.result == 'device' else out.numpy()
 
     def release(self, req):
@@ -931,6 +982,13 @@ class GpuExecutor:
         g = req.state.pop('g', None)
         if g is not None and 'block' in g:
             self.arena.free(*g['block'])
+
+    def finished_step_seconds(self):
+        """Device time of the batched steps finished so far (seconds)."""
+        while self._step_events and self._step_events[0][1].query():
+            e0, e1 = self._step_events.popleft()
+            self._step_seconds += e0.elapsed_time(e1) * 1e-3
+        return self._step_seconds
 
     def shutdown(self):
         """Wait for the GPU and give the arena back to the device."""

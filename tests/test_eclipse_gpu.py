@@ -72,3 +72,81 @@ def test_eclipse_many_pv_vs_oracle():
     want = oracle.eclipse_full(time, k, t0, p, a, inc, e, w, 0.9, np.zeros(time.size, int), [0], [4], [5 / 1440])
     assert np.sum(want < np.pi * k[:, None] ** 2 - 1e-9) > 10000
     assert _err(f, want) <= TOL
+
+
+# ---- split precision (rr_eclipse_split, rr_es_split) -------------------------
+# FP32 per-sample areas on FP32 Taylor coefficients: |dF| <= 2k |dz| + a few
+# ulps of pi k^2 with |dz| ~ 1e-7, so well inside the transit model's 1e-6
+SPLIT_TOL = 1e-6
+
+
+def test_eclipse_split_golden_and_invalid_rows(golden):
+    """Multiple light curves, epochs and supersampling, one invalid pv."""
+    import torch
+    from pytransit_gb300 import EclipseModel
+    g = golden("eclipse")
+    m = EclipseModel(precision='split')
+    m.set_data(g["time"], lcids=g["lcids"], nsamples=g["nsamples"], exptimes=g["exptimes"], epids=g["epids"])
+    f = m.evaluate(g["k"], g["t0"], g["p"], g["a"], g["inc"], g["e"], g["w"], rstar=float(g["rstar"]))
+    assert f.dtype == np.float64
+    assert _err(f, g["flux"]) <= SPLIT_TOL
+    assert np.isnan(f[5]).all()
+    t = m.evaluate(g["k"], g["t0"], g["p"], g["a"], g["inc"], g["e"], g["w"], rstar=float(g["rstar"]), copy=False)
+    assert t.dtype == torch.float32 and t.is_cuda
+
+
+def test_eclipse_split_many_pv_vs_oracle_and_fp64():
+    """BJD-scale times (the exact FP32-pair fold), eccentric orbits, 4
+    samples: split against the oracle and against the FP64 kernel."""
+    from pytransit_gb300 import EclipseModel
+    rng = np.random.default_rng(18)
+    T = 2459000.0
+    time = T + np.arange(0, 12.0, 5 / 1440)
+    npv = 300
+    k = rng.uniform(0.05, 0.2, npv)
+    t0 = T + rng.normal(0.3, 1e-3, (npv, 1))
+    p = rng.uniform(0.8, 6.0, npv)
+    a = rng.uniform(3, 15, npv)
+    inc = np.arccos(rng.uniform(0, 0.95, npv) / a)
+    e = rng.uniform(0, 0.4, npv)
+    w = rng.uniform(0, 2 * np.pi, npv)
+    want = oracle.eclipse_full(time, k, t0, p, a, inc, e, w, 0.9, np.zeros(time.size, int), [0], [4], [5 / 1440])
+    got = {}
+    for prec in ("split", "fp64"):
+        m = EclipseModel(precision=prec)
+        m.set_data(time, nsamples=[4], exptimes=[5 / 1440])
+        got[prec] = m.evaluate(k, t0, p, a, inc, e, w, rstar=0.9)
+    assert np.sum(want < np.pi * k[:, None] ** 2 - 1e-6) > 20000
+    assert _err(got["fp64"], want) <= TOL
+    assert _err(got["split"], want) <= SPLIT_TOL
+    assert _err(got["split"], got["fp64"]) <= SPLIT_TOL
+
+
+def test_es_split_golden_and_vs_oracle(golden):
+    from pytransit_gb300 import ESModel
+    g = golden("eclipse")
+    m = ESModel(precision='split')
+    m.set_data(g["es_time"], nsamples=[3], exptimes=[0.01])
+    f = m.evaluate(g["es_fratio"], g["es_k"], g["es_t0"], g["es_p"], g["es_a"], g["es_inc"], g["es_e"], g["es_w"],
+                   rstar=g["es_rstar"])
+    assert _err(f, g["es_flux"]) <= SPLIT_TOL
+    # a larger population at BJD scale, 40 channels
+    rng = np.random.default_rng(19)
+    T = 2459000.0
+    time = T + np.arange(-0.5, 5.0, 2 / 1440)
+    npv, npb = 64, 40
+    k = rng.uniform(0.05, 0.15, npv)
+    t0 = T + rng.normal(0.0, 1e-3, npv)
+    p = rng.uniform(1.0, 4.0, npv)
+    a = rng.uniform(3, 12, npv)
+    inc = np.arccos(rng.uniform(0, 0.9, npv) / a)
+    e = rng.uniform(0, 0.3, npv)
+    w = rng.uniform(0, 2 * np.pi, npv)
+    fr = rng.uniform(1e-4, 5e-3, (npv, npb))
+    want = oracle.es_full(time, k, t0, p, a, inc, e, w, 1.0, fr, 5, 2 / 1440)
+    m = ESModel(precision='split')
+    m.set_data(time, nsamples=[5], exptimes=[2 / 1440])
+    f = m.evaluate(fr, k, t0, p, a, inc, e, w)
+    assert f.shape == (npv, npb, time.size)
+    assert np.sum(want < 1 - 1e-6) > 10000
+    assert _err(f, want) <= SPLIT_TOL

@@ -196,3 +196,17 @@ def test_bench_serving_mix_and_sustained_rule():
     assert not bench.sustained(dict(run, achieved_req_per_s=1700))
     assert not bench.sustained(dict(run, queued_at_end_of_arrivals=500))
     assert not bench.sustained(dict(run, latency_p99_second_half_s=0.2))
+
+
+def test_serve_setup_args_layout_matches_the_library():
+    """rr_serve_setup_args (52 fields of 8 bytes) as the serving host fills it."""
+    import ctypes as C
+    from pytransit_gb300 import _lib
+    from pytransit_gb300.serving import SETUP_ARGS_DTYPE
+    L = _lib.lib()
+    L.rr_serve_setup_args_size.argtypes = [C.POINTER(C.c_int)]
+    L.rr_serve_setup_args_size.restype = None
+    n = C.c_int()
+    L.rr_serve_setup_args_size(C.byref(n))
+    assert n.value == SETUP_ARGS_DTYPE.itemsize == 52 * 8
+    assert SETUP_ARGS_DTYPE.names[-2:] == ('bound_host', 'desc')

@@ -285,3 +285,19 @@ def test_served_future_carries_the_error_bound():
     f.result(timeout=5)
     srv.close()
     assert f.error_bound == pytest.approx(3e-7)
+
+
+def test_ts_work_items_slices_match_the_whole():
+    from pytransit_gb300.serving import ts_work_items
+    for npv, npt in [(1, 10), (5, 128 * 33 + 1), (37, 100000)]:
+        items = ts_work_items(npv, npt)
+        whole = items[:]
+        assert whole.shape == (len(items), 4) and whole.dtype == np.int32
+        ntiles = (npt + 127) // 128
+        cover = np.zeros((npv, ntiles), int)
+        for pv0, pv1, t0, t1 in whole:
+            assert pv1 == pv0 + 1 and 0 < t1 - t0 <= 16
+            cover[pv0:pv1, t0:t1] += 1
+        assert (cover == 1).all()
+        c = len(items) // 3
+        np.testing.assert_array_equal(np.concatenate([items[:c], items[c:2 * c], items[2 * c:]]), whole)

@@ -114,3 +114,25 @@ def test_device_results_through_the_persistent_kernel():
     assert srv.stats.completed == len(reqs) and srv.stats.steps > 1
     for r, g in zip(reqs, got):
         assert close(g, reference(*r)) <= TOL
+
+
+@pytest.mark.parametrize("result", ["device", "host"])
+def test_dropped_results_resolve_to_their_point_count(result):
+    """keep_result=False (consumers that only count or time): every future
+    resolves to the request's number of model points, and the server's step
+    and busy counters advance."""
+    from pytransit_gb300.serving import RRServer
+    rng = np.random.default_rng(11)
+    reqs = [make_request(rng, 'rr', 'quadratic', 12, 2000, 1), make_request(rng, 'ts', 'power-2', 3, 1500, 5),
+            make_request(rng, 'rr', 'nonlinear', 5, 900, 10)]
+    srv = RRServer(hbm_budget=4e9, result=result, step_items=16)
+    futs = [srv.submit(*r, keep_result=False) for r in reqs]
+    got = [f.result(timeout=120) for f in futs]
+    srv.close()
+    for (kind, law, data, params), n in zip(reqs, got):
+        npv = np.asarray(params['p']).size
+        npb = np.asarray(params['k']).shape[1] if kind == 'ts' else 1
+        assert n == npv * npb * data['time'].size
+    st = srv.stats.summary()
+    assert st['completed'] == len(reqs) and st['steps'] >= 1
+    assert st['admit_s'] > 0 and st['gpu_step_s'] >= 0
