@@ -182,6 +182,28 @@ int rr_flux_split_range(const float *times_ff, int npt, const int32_t *lcids, in
                         double dg, const void *workspace, int pv0, int pv1, float *flux, int ldflux,
                         void *stream);
 
+/* rr_flux_split_range that stores only what can differ from 1: the 128-point
+ * tiles whose times reach a transit window (every point of such a tile) and
+ * the NaN rows of invalid parameter vectors.  Every other point of
+ * flux[pv1 - pv0, ldflux] must already hold 1.0, the value the reference
+ * gives every point outside the bounding box (model_full.py:90-91).  flux
+ * may be device memory or page-locked host
+ * memory (cudaHostAlloc / cudaHostRegister), which the kernel writes through
+ * its device address; pageable host memory is rejected (RR_ERR_ARG).  With
+ * rr_host_fill_f32 this moves one bit per culled tile instead of its 512
+ * bytes: the host sets a chunk of rows to 1 while the GPU writes the transit
+ * tiles of the chunk before it. */
+int rr_flux_split_transits(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb,
+                           int ng, double dg, const void *workspace, int pv0, int pv1, float *flux, int ldflux,
+                           void *stream);
+
+/* Host memory fill on the library's own threads: dst[0..n) = value, split
+ * over nthreads threads (the calling thread included; nthreads <= 0 or 1:
+ * the calling thread alone).  The threads are started on first use and kept;
+ * a process forked after that starts its own.  No GPU work.  Returns 0, or
+ * RR_ERR_ARG for dst NULL with n > 0. */
+int rr_host_fill_f32(float *dst, size_t n, float value, int nthreads);
+
 /* ---- transmission-spectroscopy model --------------------------------------- */
 
 /* Replaces tsmodel_serial (pytransit/models/roadrunner/model_trspec.py:12-93)

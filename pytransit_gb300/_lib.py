@@ -57,6 +57,8 @@ def _sig(L):
                                        _vp, _vp, _vp, _vp, _sz, _vp])
     L.rr_flux_split.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _vp, _i, _vp]
     L.rr_flux_split_range.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
+    L.rr_flux_split_transits.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
+    L.rr_host_fill_f32.argtypes = [_vp, _sz, C.c_float, _i]
     L.rr_ts_workspace_bytes.argtypes = [_i, _i, _i, _i]
     L.rr_ts_workspace_bytes.restype = _sz
     _ts_tail = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _d,

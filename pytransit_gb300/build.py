@@ -60,7 +60,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

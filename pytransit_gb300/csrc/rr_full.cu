@@ -614,6 +614,7 @@ struct FluxSplitArgs {
   int npt, npv, npb, nlc, ng, ldflux;
   float inv_dg;
   float* flux;
+  int transits_only;   // store only the tiles that reach a transit (and invalid rows); the rest holds 1
 };
 
 constexpr int LC_SMEM = 64;                  // light-curve records staged in shared memory
@@ -983,9 +984,10 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
     const int jn = min(32, ntl - j0);
     const unsigned jmask = jn == 32 ? 0xffffffffu : (1u << jn) - 1u;
     const unsigned cmask = __ballot_sync(FULL, cull) & jmask;
-    // the culled tiles first, walking the set bits of the mask
+    // the culled tiles first, walking the set bits of the mask (none when the
+    // caller has already set the row to 1; an invalid pv's NaN always)
     float4* const row4 = reinterpret_cast<float4*>(row) + lane;
-    for (unsigned m = cmask; m; m &= m - 1u) {
+    for (unsigned m = (A.transits_only && valid) ? 0u : cmask; m; m &= m - 1u) {
       const int tile = tw0 + (j0 + __ffs(m) - 1) * t_step;
       if (row_vec && tile != tile_part) {
         __stcs(row4 + (size_t)tile * (WARP_TILE / 4), fill4);
@@ -1299,9 +1301,9 @@ int rr_flux_split(const float* times_ff, int npt, const int32_t* lcids, int npv,
   return rr_flux_split_range(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, 0, npv, flux, ldflux, stream);
 }
 
-int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
-                        double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
-                        void* stream) {
+static int flux_split_launch(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb,
+                             int ng, double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
+                             void* stream, int transits_only) {
   if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || ldflux < npt) return RR_ERR_ARG;
   if (pv0 < 0 || pv1 > npv || pv0 > pv1) return RR_ERR_ARG;
   if (pv1 == pv0 || npt == 0) return RR_OK;
@@ -1315,7 +1317,7 @@ int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, in
   fa.ldm = t.ldm + (size_t)pv0 * npb * ng;
   npv = pv1 - pv0;
   fa.npt = npt; fa.npv = npv; fa.npb = npb; fa.nlc = nlc; fa.ng = ng; fa.ldflux = ldflux;
-  fa.inv_dg = (float)(1.0 / dg); fa.flux = flux;
+  fa.inv_dg = (float)(1.0 / dg); fa.flux = flux; fa.transits_only = transits_only;
   // tile ranges of FLUX_CHUNK tiles, shorter when the launch would otherwise
   // have fewer than about four blocks per resident warp slot (SMs x 32)
   const int ntiles = (npt + WARP_TILE - 1) / WARP_TILE;
@@ -1331,6 +1333,34 @@ int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, in
   else
     flux_split_kernel<false><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
   return check_launch("rr_flux_split");
+}
+
+int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
+                        double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
+                        void* stream) {
+  return flux_split_launch(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, pv0, pv1, flux, ldflux, stream,
+                           0);
+}
+
+int rr_flux_split_transits(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
+                           double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
+                           void* stream) {
+  if (!flux) return RR_ERR_ARG;
+  // page-locked host rows are written through their device address
+  cudaPointerAttributes at{};
+  const cudaError_t e = cudaPointerGetAttributes(&at, flux);
+  if (e != cudaSuccess) {
+    set_cuda_error(e, "rr_flux_split_transits (pointer)");
+    return RR_ERR_CUDA;
+  }
+  float* dst = nullptr;
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)
+    dst = flux;
+  else if (at.type == cudaMemoryTypeHost)
+    dst = static_cast<float*>(at.devicePointer);
+  if (!dst) return RR_ERR_ARG;   // pageable host memory: not reachable by the kernel here
+  return flux_split_launch(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, pv0, pv1, dst, ldflux, stream,
+                           1);
 }
 
 int rr_full_split(const float* times_ff, double t_ref, double t_absmax, int npt, const double* k, int nkc,

@@ -21,6 +21,7 @@ or garbles its input:
 * the LD-table index is clamped at g in [1 - 1e-7, 1].
 """
 import ctypes as C
+import os
 from typing import Callable, List, Tuple, Union
 from warnings import warn
 
@@ -50,6 +51,16 @@ def create_z_grid(zcut: float, nin: int, nedge: int):
     for i in range(nin + nedge - 1):
         z_means[i + 1] = 0.5 * (z_edges[i] + z_edges[i + 1])
     return z_edges, z_means
+
+
+def _default_host_threads():
+    """Host threads for output fills: the CPUs this process may run on, at most 16
+    (a fill saturates the host memory well before that)."""
+    try:
+        n = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        n = os.cpu_count() or 1
+    return max(1, min(16, n))
 
 
 class RoadRunnerModel(TransitModel):
@@ -92,6 +103,13 @@ class RoadRunnerModel(TransitModel):
             raise ValueError("precision must be 'fp64' or 'split'")
         self.precision = precision
         self.device = device
+        # Pinned host output of the split path: part of the rows copied over
+        # from the device while the host sets the others to 1 on host_threads
+        # threads and the GPU writes only their transit tiles (host_fill True),
+        # or the whole flux copied over in chunks (False).
+        self.host_fill = True
+        self.host_threads = _default_host_threads()
+        self.host_fill_fraction = 0.5   # share of the rows set to 1 by the host (the rest copied over)
 
         # Limb darkening model (rrmodel.py:109-131)
         self.ld_law = None           # device law id of a named law, else None
@@ -337,6 +355,53 @@ class RoadRunnerModel(TransitModel):
         comp.wait_stream(cs)
         return 0
 
+    def _flux_to_pinned(self, dd, npt, npv, nlc, npb, ws, out2d, device, nchunks=4):
+        """Split-path flux into the pinned host rows out2d[npv, npt] over the
+        host link and the host's own memory bandwidth at once.  The first
+        rows (a 1 - host_fill_fraction share) are computed on the device in
+        one launch and copied over on a copy stream.  Meanwhile the host sets
+        the other rows to 1, a pv chunk at a time, on the library's threads
+        (rr_host_fill_f32), and after each chunk the GPU writes that chunk's
+        transit tiles and invalid rows straight into it
+        (rr_flux_split_transits): tiles that reach no transit window never
+        cross the link.  The current stream waits for the copy; the caller
+        synchronises it.  Returns the first non-zero status."""
+        import torch
+        from . import _lib
+        L, P = _lib.lib(), _lib.ptr
+        comp = torch.cuda.current_stream(device)
+        sp = C.c_void_p(comp.cuda_stream)
+        ncopy = int(round(npv * (1.0 - min(1.0, max(0.0, float(self.host_fill_fraction))))))
+        cs = None
+        if ncopy > 0:
+            key = (device, ncopy, npt)
+            if getattr(self, '_stage', None) is None or self._stage[0] != key:
+                self._stage = (key, torch.empty((ncopy, npt), dtype=torch.float32, device=device),
+                               torch.cuda.Stream(device))
+            _, buf, cs = self._stage
+            st = L.rr_flux_split_range(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg,
+                                       P(ws), 0, ncopy, P(buf), npt, sp)
+            if st != 0:
+                return st
+            cs.wait_stream(comp)
+            with torch.cuda.stream(cs):
+                out2d[:ncopy].copy_(buf, non_blocking=True)
+        base = out2d.data_ptr()
+        nfill = npv - ncopy
+        bounds = ncopy + np.linspace(0, nfill, min(nchunks, nfill) + 1).astype(int) if nfill > 0 else []
+        for c in range(len(bounds) - 1):
+            pv0, pv1 = int(bounds[c]), int(bounds[c + 1])
+            rows = C.c_void_p(base + pv0 * npt * 4)
+            st = L.rr_host_fill_f32(rows, (pv1 - pv0) * npt, 1.0, int(self.host_threads))
+            if st == 0:
+                st = L.rr_flux_split_transits(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng,
+                                              self.dg, P(ws), pv0, pv1, rows, npt, sp)
+            if st != 0:
+                return st
+        if cs is not None:
+            comp.wait_stream(cs)
+        return 0
+
     def evaluate(self, k: Union[float, ndarray], ldc: Union[ndarray, List], t0: Union[float, ndarray],
                  p: Union[float, ndarray], a: Union[float, ndarray], i: Union[float, ndarray],
                  e: Union[float, ndarray] = 0.0, w: Union[float, ndarray] = 0.0, copy: bool = True,
@@ -350,7 +415,10 @@ class RoadRunnerModel(TransitModel):
         [npv, npt] torch tensor (pinned host memory or device) that receives the
         flux; it is filled, synchronised and returned.  In the split path a
         contiguous pinned host float32 tensor is filled in parameter-vector
-        chunks, each copied to the host while the next one is computed.
+        chunks: the host sets a chunk's rows to 1 (``host_threads`` threads)
+        while the GPU writes the tiles of the chunk before it that reach a
+        transit window straight into that memory, so the out-of-transit
+        points never cross the host link.
 
         return_error=True returns (flux, bound): the stated maximum absolute
         flux error of this result against the FP64 model (see
@@ -462,7 +530,8 @@ class RoadRunnerModel(TransitModel):
                                         self.nk, self.ng, nz, self.dk, kmin, kmax, P(tb['ze']), P(ws), ws.numel(),
                                         stream, self.ld_law or 0, P(ldc_d), npar, P(basis), nb)
             if st == 0 and pipe:
-                st = self._flux_to_host(dd, npt, npv, nlc, npb, ws, user_out.view(npv, npt), device)
+                to_host = self._flux_to_pinned if self.host_fill else self._flux_to_host
+                st = to_host(dd, npt, npv, nlc, npb, ws, user_out.view(npv, npt), device)
             elif st == 0:
                 st = L.rr_flux_split(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg,
                                      P(ws), P(res), ldf, stream)

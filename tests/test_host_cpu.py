@@ -210,3 +210,64 @@ def test_serve_setup_args_layout_matches_the_library():
     L.rr_serve_setup_args_size(C.byref(n))
     assert n.value == SETUP_ARGS_DTYPE.itemsize == 52 * 8
     assert SETUP_ARGS_DTYPE.names[-2:] == ('bound_host', 'desc')
+
+
+def test_host_fill_sizes_and_threads():
+    """rr_host_fill_f32 writes exactly dst[0..n), for any size and thread count
+    (the slices are 64-byte blocks, the last one partial)."""
+    from pytransit_gb300 import _lib
+    L = _lib.lib()
+    for n in (0, 1, 15, 17, 1000, 65535, 65536, 65537, (1 << 20) + 3):
+        for nt in (0, 1, 2, 3, 8, 16):
+            a = np.full(n + 32, -7.0, np.float32)
+            assert L.rr_host_fill_f32(ctypes.c_void_p(a.ctypes.data + 64), n, 1.0, nt) == 0
+            assert (a[:16] == -7).all() and (a[16:16 + n] == 1.0).all() and (a[16 + n:] == -7).all(), (n, nt)
+    assert L.rr_host_fill_f32(None, 10, 1.0, 4) == 2
+    assert L.rr_host_fill_f32(None, 0, 1.0, 4) == 0
+
+
+def test_host_fill_from_several_threads_and_after_fork():
+    """Calls from several Python threads are serialised and each fills its own
+    buffer; a process forked after the pool started fills on a pool of its own
+    (it would wait forever on the parent's threads otherwise)."""
+    import threading
+    from pytransit_gb300 import _lib
+    L = _lib.lib()
+    n = 1 << 21
+    bufs = [np.zeros(n, np.float32) for _ in range(6)]
+
+    def go(j):
+        for _ in range(5):
+            assert L.rr_host_fill_f32(ctypes.c_void_p(bufs[j].ctypes.data), n, float(j + 1), 4) == 0
+
+    ts = [threading.Thread(target=go, args=(j,)) for j in range(len(bufs))]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(60)
+    for j, b in enumerate(bufs):
+        assert (b == j + 1).all()
+    if not hasattr(os, "fork"):
+        return
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", DeprecationWarning)   # the multi-threaded fork is the case tested
+        pid = os.fork()
+    if pid == 0:   # child: its own pool, then exit without running the test harness's teardown
+        ok = False
+        try:
+            c = np.zeros(n, np.float32)
+            ok = L.rr_host_fill_f32(ctypes.c_void_p(c.ctypes.data), n, 3.0, 4) == 0 and bool((c == 3.0).all())
+        finally:
+            os._exit(0 if ok else 1)
+    import time
+    t_end = time.time() + 60
+    while time.time() < t_end:
+        done, status = os.waitpid(pid, os.WNOHANG)
+        if done:
+            assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0
+            return
+        time.sleep(0.05)
+    os.kill(pid, 9)
+    os.waitpid(pid, 0)
+    raise AssertionError("the forked child's fill did not finish")

@@ -221,28 +221,107 @@ def test_device_output_and_copy_false():
     assert out.dtype == torch.float32
 
 
-@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("precision,host_fill,fraction", [("fp64", True, 0.6), ("split", True, 0.6),
+                                                            ("split", True, 0.0), ("split", True, 1.0),
+                                                            ("split", False, 0.6)])
 @pytest.mark.parametrize("npt", [1000, 1003])
-def test_pinned_host_output(precision, npt):
-    """out= a pinned host tensor: the split path computes it in pv chunks and
-    copies each chunk while the next is computed (also for npt not a multiple
-    of 4 and uneven chunks); same values as the device result, and a second
-    call overwrites every element."""
+def test_pinned_host_output(precision, host_fill, fraction, npt):
+    """out= a pinned host tensor.  With host_fill, the split path copies the
+    first rows over from the device while the host sets the others (a
+    host_fill_fraction share) to 1, a pv chunk at a time, and the GPU writes
+    only their tiles that reach a transit (and the NaN rows of invalid
+    vectors) straight into them; without, every chunk is computed on the
+    device and copied over while the next is computed.  Also for npt not a
+    multiple of 4 and uneven chunks: the same bits as the device result, and
+    a second call overwrites every element."""
     import torch
     rng = np.random.default_rng(3)
     T = 2459000.0
     time = T + np.linspace(-0.3, 0.3, npt)
     npv = 37
+    a = rng.uniform(5, 9, npv)
+    a[[4, 30]] = 0.9                    # invalid vectors (a <= 1): NaN rows
     args = (rng.uniform(0.08, 0.12, (npv, 1)), [0.3, 0.1], T + rng.normal(0, 1e-3, (npv, 1)),
-            rng.uniform(1, 3, npv), rng.uniform(5, 9, npv), np.full(npv, 1.54), 0.0, 0.0)
+            rng.uniform(1, 3, npv), a, np.full(npv, 1.54), 0.0, 0.0)
     m = rr(precision=precision)
+    m.host_fill = host_fill
+    m.host_fill_fraction = fraction
     m.set_data(time)
     want = m.evaluate(*args, copy=False).cpu()
+    assert torch.isnan(want[4]).all() and torch.isnan(want[30]).all()
     dt = torch.float32 if precision == 'split' else torch.float64
     out = torch.full((npv, npt), -7.0, dtype=dt, pin_memory=True)
     got = m.evaluate(*args, out=out)
     assert got is out
-    assert torch.equal(out, want.to(dt))
+    torch.testing.assert_close(out, want.to(dt), rtol=0, atol=0, equal_nan=True)
     out.fill_(-7.0)
     m.evaluate(*args, out=out)
-    assert torch.equal(out, want.to(dt))
+    torch.testing.assert_close(out, want.to(dt), rtol=0, atol=0, equal_nan=True)
+
+
+def test_flux_split_transits_writes_only_transit_tiles():
+    """rr_flux_split_transits through the C ABI on a device buffer: where the
+    buffer holds 1 it gives the same bits as rr_flux_split_range; where it
+    holds a sentinel, only whole 128-point tiles are written (every point of a
+    written tile, the sentinel untouched elsewhere), every point that differs
+    from 1 lies in a written tile, and the NaN row of an invalid vector is
+    written in full.  Pageable host memory is refused."""
+    import ctypes as C
+    import torch
+    from pytransit_gb300 import _lib
+    rng = np.random.default_rng(11)
+    T = 2459000.0
+    npt, npv = 19700, 64
+    time = T + np.arange(npt) * (2.0 / 1440.0)
+    a = rng.uniform(3, 20, npv)
+    a[7] = 0.5
+    args = (rng.uniform(0.05, 0.15, (npv, 1)), [0.3, 0.1], T + rng.normal(0, 1e-3, (npv, 1)),
+            rng.uniform(0.5, 15, npv), a, np.arccos(rng.uniform(0, 0.9, npv) / np.maximum(a, 1)), 0.0, 0.0)
+    m = rr(precision='split')
+    m.set_data(time)
+    full = m.evaluate(*args, copy=False)          # leaves the model's split workspace prepared
+    st = m._bound_state
+    dev = st['device']
+    dd = m._device_data(dev)
+    L, P = _lib.lib(), _lib.ptr
+    sp = _lib.stream_ptr(dev)
+
+    def transits(buf, pv0=0, pv1=npv):
+        return L.rr_flux_split_transits(P(dd['times_ff']), npt, P(dd['lcids']), npv, st['nlc'], st['npb'], m.ng,
+                                        m.dg, P(st['ws']), pv0, pv1, C.c_void_p(buf.data_ptr()), npt, sp)
+
+    ones = torch.ones((npv, npt), dtype=torch.float32, device=dev)
+    assert transits(ones) == 0
+    torch.cuda.synchronize()
+    torch.testing.assert_close(ones, full, rtol=0, atol=0, equal_nan=True)
+    sentinel = -3.0
+    sb = torch.full((npv, npt), sentinel, dtype=torch.float32, device=dev)
+    assert transits(sb) == 0
+    torch.cuda.synchronize()
+    sbh, fh = sb.cpu().numpy(), full.cpu().numpy()
+    ntile = (npt + 127) // 128
+    pad = np.full((npv, ntile * 128), sentinel, np.float32)
+    pad[:, :npt] = sbh
+    real = (np.arange(ntile * 128) < npt).reshape(ntile, 128)       # the last tile is partial
+    held = (pad.reshape(npv, ntile, 128) == sentinel) & real
+    written = ~held.any(-1)
+    assert ((held | ~real).all(-1) | written).all(), "a tile was written in part"
+    fpad = np.ones((npv, ntile * 128), np.float32)
+    fpad[:, :npt] = fh
+    differs = ~(fpad.reshape(npv, ntile, 128) == 1.0).all(-1)
+    assert not (differs & ~written).any(), "a point that differs from 1 was not written"
+    w = np.repeat(written, 128, axis=1)[:, :npt]
+    np.testing.assert_array_equal(sbh[w], fh[w])
+    assert written[7].all() and np.isnan(sbh[7]).all()
+    assert 0 < written.mean() < 0.5
+    # a pv sub-range writes only its own rows
+    sr = torch.full((npv, npt), sentinel, dtype=torch.float32, device=dev)
+    assert L.rr_flux_split_transits(P(dd['times_ff']), npt, P(dd['lcids']), npv, st['nlc'], st['npb'], m.ng, m.dg,
+                                    P(st['ws']), 10, 20, C.c_void_p(sr[10].data_ptr()), npt, sp) == 0
+    torch.cuda.synchronize()
+    srh = sr.cpu().numpy()
+    assert (srh[:10] == sentinel).all() and (srh[20:] == sentinel).all()
+    np.testing.assert_array_equal(srh[10:20], sbh[10:20])
+    pageable = np.ones((npv, npt), np.float32)
+    assert L.rr_flux_split_transits(P(dd['times_ff']), npt, P(dd['lcids']), npv, st['nlc'], st['npb'], m.ng,
+                                    m.dg, P(st['ws']), 0, npv, C.c_void_p(pageable.ctypes.data), npt, sp) == 2
