@@ -167,6 +167,38 @@ def test_taylor_orbit_matches_exact_kepler():
     assert worst < 1e-4, worst
 
 
+@pytest.mark.parametrize("eccentric,bound", [(False, 2e-5), (True, 2e-4)])
+def test_taylor_orbit_flux_truncation(eccentric, bound):
+    """The flux the orbit layer's truncation moves, reported at the flux level:
+    over the bounding box of 400 orbits drawn as the bench workloads draw them
+    (k ~ U(0.05, 0.15), p ~ U(0.5, 15), a ~ U(3, 20), b ~ U(0, 0.9); circular
+    as the plain-path workload, e ~ U(0, 0.3) as the precision workload), the
+    quadratic-LD flux (the Mandel & Agol model, a smooth function of z) at the
+    Taylor z against the same flux at the exact Kepler z.  Measured: circular
+    max 4.8e-6 (median 1.1e-8), eccentric max 4.9e-5 (median 1.4e-8), from the
+    shortest, closest orbits, where the transit lasts a larger part of the
+    period.  This is the degree-4 series itself (meepmeep's), shared by the
+    reference's RoadRunner path, not an error of this build against it."""
+    rng = np.random.default_rng(7)
+    worst, per_orbit = 0.0, []
+    for _ in range(400):
+        k = rng.uniform(0.05, 0.15)
+        p, a = rng.uniform(0.5, 15), rng.uniform(3, 20)
+        e, w = (rng.uniform(0, 0.3), rng.uniform(0, 2 * np.pi)) if eccentric else (0.0, 0.0)
+        inc = np.arccos(rng.uniform(0, 0.9) / a)
+        c = oracle.solve2d(0.0, p, a, inc, e, w)
+        t1, t4 = oracle.bounding_box(k, c)
+        ts = np.linspace(t1, t4, 201)
+        zt = np.array([oracle.sep_c(t, c) for t in ts])
+        zk = np.array([abs(oracle.z_kepler(t, 0.0, p, a, inc, e, w)) for t in ts])
+        d = np.abs(oracle.ma_quad_z(zt, k, 0.4, 0.2) - oracle.ma_quad_z(zk, k, 0.4, 0.2)).max()
+        worst = max(worst, d)
+        per_orbit.append(d)
+    print(f"Taylor vs exact Kepler, flux: max {worst:.2e}, median {np.median(per_orbit):.2e}")
+    assert worst < bound
+    assert np.median(per_orbit) < 1e-7
+
+
 def test_mandel_agol_cross_check():
     """tests/test_ma_quadratic_nb.py:39-55 pins the analytic quadratic model for
     k = 0.1, u = (0.2, 0.1).  RoadRunner's table model at the same z agrees to
