@@ -153,7 +153,7 @@ es_flux_kernel(const double* __restrict__ times, int npt, const double* __restri
 // the samples of the in-box points in FP32.
 // ---------------------------------------------------------------------------
 constexpr int ECL32 = 16;   // c[0..9], [10] p_hi, [11] p_lo, [12] 1/p_hi, [13] k, [14] flags, [15] pi k^2
-constexpr int ECL_NW = 4;   // warps per block of the split flux kernels
+constexpr int ECL_NW = 2;   // warps per block of the split flux kernels
 constexpr int ECL_CHUNK = 32;
 
 struct EclSplitArgs {
@@ -295,12 +295,17 @@ __global__ void __launch_bounds__(ECL_NW * 32) eclipse_flux_split_kernel(EclSpli
                                                        time_meta_offset(A.npt));
   const int ntiles = (A.npt + TIME_TILE - 1) / TIME_TILE;
   const int tb0 = blockIdx.x * chunk, tb1 = min(ntiles, tb0 + chunk);
-  for (int tile = tb0 + warp; tile < tb1; tile += ECL_NW) {
-    // the tile's cull test, by lane 0 and broadcast: its time range against
-    // the box copies around it (as the transit flux kernel's)
+  // The warp's tiles are tw0 + j ECL_NW, j < ntl, tested 32 at a time (one
+  // per lane, as the transit flux kernel does); the culled ones are stored
+  // first, walking the set bits of the cull mask, then the others point by
+  // point.
+  const int tw0 = tb0 + warp;
+  const int ntl = tw0 < tb1 ? (tb1 - tw0 + ECL_NW - 1) / ECL_NW : 0;
+  const unsigned FULL = 0xffffffffu;
+  for (int j0 = 0; j0 < ntl; j0 += 32) {
     bool cull = !valid;
-    if (valid && !wide) {
-      const float4 tm = __ldg(meta + tile);
+    if (valid && !wide && j0 + lane < ntl) {
+      const float4 tm = __ldg(meta + tw0 + (j0 + lane) * ECL_NW);
       const int tlc = ES ? 0 : __float_as_int(tm.z);   // ES: one record for every point
       if (tlc >= 0) {
         const float* R = LCR + tlc * LC32;
@@ -315,9 +320,12 @@ __global__ void __launch_bounds__(ECL_NW * 32) eclipse_flux_split_kernel(EclSpli
         cull = !hit;
       }
     }
-    const int p0 = tile * TIME_TILE;
-    const bool full = p0 + TIME_TILE <= A.npt;
-    if (cull) {
+    const int jn = min(32, ntl - j0);
+    const unsigned jmask = jn == 32 ? FULL : (1u << jn) - 1u;
+    const unsigned cmask = __ballot_sync(FULL, cull) & jmask;
+    for (unsigned m = cmask; m; m &= m - 1u) {
+      const int p0 = (tw0 + (j0 + __ffs(m) - 1) * ECL_NW) * TIME_TILE;
+      const bool full = p0 + TIME_TILE <= A.npt;
       for (int b = 0; b < nrow; ++b) {
         float* row = fpv + (size_t)b * A.ldflux;
         if (vec && full) {
@@ -327,32 +335,34 @@ __global__ void __launch_bounds__(ECL_NW * 32) eclipse_flux_split_kernel(EclSpli
             if (p0 + q * 32 + lane < A.npt) __stcs(row + p0 + q * 32 + lane, outv);
         }
       }
-      continue;
     }
-    // slot q of lane l: point p0 + q * 32 + l
-    float val[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int pt = p0 + q * 32 + lane;
-      val[q] = ES ? 0.0f : outv;   // ES: the mean area (0 outside the box)
-      if (pt >= A.npt || !valid) continue;
-      const float2 tt = __ldg(A.times_ff + pt);
-      const float* R = ES ? LCR : LCR + __ldg(A.lcids + pt) * LC32;
-      const float sv = tt.x - R[LC_D0H];
-      const float n = floorf(fmaf(sv, inv_p, 0.5f));
-      const float r = fmaf(-n, p_hi, sv);
-      if (wide || (r >= R[LC_FLO] && r <= R[LC_FHI])) {
-        const float t = exact_tc(tt.x, tt.y, R[LC_D0H], R[LC_D0L], n, p_hi, p_lo);
-        if (R[LC_LO] <= t && t <= R[LC_HI]) val[q] = ecl_point<ES>(orb, R, t);
-      }
-    }
-    for (int b = 0; b < nrow; ++b) {
-      float* row = fpv + (size_t)b * A.ldflux;
-      const float c = ES ? cbs[b] : 0.0f;
+    for (unsigned m = ~cmask & jmask; m; m &= m - 1u) {
+      const int p0 = (tw0 + (j0 + __ffs(m) - 1) * ECL_NW) * TIME_TILE;
+      // slot q of lane l: point p0 + q * 32 + l
+      float val[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int pt = p0 + q * 32 + lane;
-        if (pt < A.npt) __stcs(row + pt, ES ? (valid ? 1.0f - c * val[q] : outv) : val[q]);
+        val[q] = ES ? 0.0f : outv;   // ES: the mean area (0 outside the box)
+        if (pt >= A.npt || !valid) continue;
+        const float2 tt = __ldg(A.times_ff + pt);
+        const float* R = ES ? LCR : LCR + __ldg(A.lcids + pt) * LC32;
+        const float sv = tt.x - R[LC_D0H];
+        const float n = floorf(fmaf(sv, inv_p, 0.5f));
+        const float r = fmaf(-n, p_hi, sv);
+        if (wide || (r >= R[LC_FLO] && r <= R[LC_FHI])) {
+          const float t = exact_tc(tt.x, tt.y, R[LC_D0H], R[LC_D0L], n, p_hi, p_lo);
+          if (R[LC_LO] <= t && t <= R[LC_HI]) val[q] = ecl_point<ES>(orb, R, t);
+        }
+      }
+      for (int b = 0; b < nrow; ++b) {
+        float* row = fpv + (size_t)b * A.ldflux;
+        const float c = ES ? cbs[b] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int pt = p0 + q * 32 + lane;
+          if (pt < A.npt) __stcs(row + pt, ES ? (valid ? 1.0f - c * val[q] : outv) : val[q]);
+        }
       }
     }
   }
