@@ -164,9 +164,72 @@ struct EclSplitArgs {
   float* flux;
 };
 
-// One pv: FP64 shift, light travel time and jet about mid-eclipse, rounded to
-// FP32; contacts by FP32 bisection on the FP32 coefficients (they only place
-// the box, padded by pad0 + exptime).  For the spectroscopic model (ES),
+// The split path's mid-eclipse orbit, for one pv.
+//
+// The eclipse offset stays FP64, because it is added to t0.  One FP64 sincos
+// of w stands in for the four trigonometric calls of eclipse_time_offset
+// (sin(pi/2 - w) = cos w and so on), and a circular orbit takes p/2 without
+// any.  The light travel time is FP32: it is ~1e-4 d, so its rounding is
+// ~1e-11 d.
+//
+// The jet is about the eclipse conjunction, f = 3 pi/2 - w.  solve2d_phase
+// reaches the same Keplerian state by a Newton solve from the mean anomaly at
+// mid-transit plus n times the offset.  Here the state is taken in closed
+// form, as solve2d_conj_f32 takes the transit's, and it is in FP32:
+//   r  = a (1 - e^2) / (1 - e sin w)
+//   vr = -n a e cos w / sqrt(1 - e^2)
+//   vt = n a (1 - e sin w) / sqrt(1 - e^2)
+// with w + f = 3 pi/2, so P0 = (0, -r) and P1 = (vt, -vr).  This agrees with
+// the FP64 Newton route to ~2e-15 relative, far below the FP32 rounding of
+// the coefficients.
+__device__ inline double eclipse_time_offset_split(double p, double e, double w) {
+  if (e == 0.0) return 0.5 * p;
+  double sw, cw;
+  sincos(w, &sw, &cw);
+  const double se = sqrt(1.0 - e * e);
+  const double etr = atan2(se * cw, e + sw);      // f = pi/2 - w: sin f = cos w, cos f = sin w
+  const double eec = atan2(-se * cw, e - sw);     // f = 3 pi/2 - w: sin f = -cos w, cos f = -sin w
+  const double mtr = etr - e * sin(etr), mec = eec - e * sin(eec);
+  const double ph = (mec - mtr) * p / (2.0 * PI);
+  return ph > 0.0 ? ph : p + ph;
+}
+
+__device__ inline float eclipse_ltt_f32(float a, float inc_sin, float e, float sw, float rstar) {
+  const float r_tr = a * (1.0f - e * e) / (1.0f + e * sw);
+  const float r_ec = a * (1.0f - e * e) / (1.0f - e * sw);
+  return (r_tr + r_ec) * inc_sin * rstar * (float)(6.957e8 / 299792458.0 / 86400.0);
+}
+
+__device__ inline void solve2d_ecl_f32(double p, double a, double inc, double e, float sw, float cw, float* c) {
+  const float af = (float)a, ef = (float)e;
+  const float n = (float)(2.0 * PI) / (float)p;
+  const float se = sqrtf(1.0f - ef * ef);
+  const float r = af * (1.0f - ef * ef) / (1.0f - ef * sw);
+  const float vr = -n * af * ef * cw / se;
+  const float vt = n * af * (1.0f - ef * sw) / se;
+  const float P0x = 0.0f, P0y = -r;
+  const float P1x = vt, P1y = -vr;
+  const float mu = n * n * af * af * af;
+  const float alpha = -1.5f;
+  const float q0 = P0x * P0x + P0y * P0y;
+  const float q1 = 2.0f * (P0x * P1x + P0y * P1y);
+  const float s0 = 1.0f / (q0 * sqrtf(q0));
+  const float P2x = -mu * s0 * P0x / 2.0f, P2y = -mu * s0 * P0y / 2.0f;
+  const float s1 = alpha * q1 * s0 / q0;
+  const float P3x = -mu * (s0 * P1x + s1 * P0x) / 6.0f;
+  const float P3y = -mu * (s0 * P1y + s1 * P0y) / 6.0f;
+  const float q2 = 2.0f * (P0x * P2x + P0y * P2y) + (P1x * P1x + P1y * P1y);
+  const float s2 = ((alpha - 1.0f) * q1 * s1 + 2.0f * alpha * q2 * s0) / (2.0f * q0);
+  const float P4x = -mu * (s0 * P2x + s1 * P1x + s2 * P0x) / 12.0f;
+  const float P4y = -mu * (s0 * P2y + s1 * P1y + s2 * P0y) / 12.0f;
+  const float ci = sinf((float)(0.5 * PI - inc));   // cos i from the small angle, as solve2d_conj_f32
+  c[0] = -P0x; c[1] = -P1x; c[2] = -P2x; c[3] = -P3x; c[4] = -P4x;
+  c[5] = -ci * P0y; c[6] = -ci * P1y; c[7] = -ci * P2y; c[8] = -ci * P3y; c[9] = -ci * P4y;
+}
+
+// One pv: the FP64 eclipse offset, the FP32 light travel time and jet about
+// mid-eclipse (above); contacts by FP32 bisection on the FP32 coefficients
+// (they only place the box, padded by pad0 + exptime).  For the spectroscopic model (ES),
 // nsamples and exptimes are null and its one record takes ns0 and ex0; the
 // channel factors are written too.
 __global__ void eclipse_prepare_split_kernel(const double* __restrict__ k, const double* __restrict__ t0, int ldt0,
@@ -189,11 +252,11 @@ __global__ void eclipse_prepare_split_kernel(const double* __restrict__ k, const
   double shift = 0.0, ltt = 0.0;
   float t1 = 0.0f, t4 = 0.0f;
   if (valid) {
-    shift = eclipse_time_offset(pp, e[pv], w[pv]);
-    ltt = eclipse_ltt(a[pv], inc[pv], e[pv], w[pv], rstar[pv]);
-    double c[10];
-    solve2d_phase(shift, pp, a[pv], inc[pv], e[pv], w[pv], c);
-    for (int i = 0; i < 10; ++i) cf[i] = (float)c[i];
+    shift = eclipse_time_offset_split(pp, e[pv], w[pv]);
+    float sw = 0.0f, cw = 1.0f;
+    if (e[pv] != 0.0) sincosf((float)w[pv], &sw, &cw);
+    ltt = (double)eclipse_ltt_f32((float)a[pv], sinf((float)inc[pv]), (float)e[pv], sw, (float)rstar[pv]);
+    solve2d_ecl_f32(pp, a[pv], inc[pv], e[pv], sw, cw, cf);
     contact_points14_f32((float)kk, cf, t1, t4);
   } else {
     for (int i = 0; i < 10; ++i) cf[i] = 0.0f;
