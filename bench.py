@@ -975,6 +975,29 @@ def main():
     d2h = ncopy * npt * 4 + int((sent[ncopy:] != -3.0).sum().item()) * 4
     del sent
 
+    # the drop-in's default call, evaluate(...) -> numpy float64 (copy=True),
+    # in both precisions: what a user of the reference gets by swapping the
+    # class; the result of each call is released before the next (as a
+    # sampler loop does), so the pinned host buffer is reused
+    def default_call(m):
+        out = None
+        for _ in range(2):
+            out = m.evaluate(*(e2e_prm[n] for n in ("k", "ldc", "t0", "p", "a", "i", "e", "w")))
+        del out
+        ts = []
+        for _ in range(max(3, e2e_steps // 2)):
+            t = time.perf_counter()
+            out = m.evaluate(*(e2e_prm[n] for n in ("k", "ldc", "t0", "p", "a", "i", "e", "w")))
+            ts.append(time.perf_counter() - t)
+            del out
+        return statistics.median(ts)
+
+    dc_split = default_call(model)
+    model64 = RoadRunnerModel('quadratic', device=device)
+    model64.set_data(**data)
+    dc_fp64 = default_call(model64)
+    del model64
+
     # --- roofline of the flux kernel ---
     kern_avg_s = statistics.mean(kern_ms) / 1e3
     s_out, s_tab = 4, 4
@@ -1008,6 +1031,11 @@ def main():
                           "into the pinned rows (d2h_bytes_per_step counts both); the result equals the "
                           "device-resident flux bit for bit",
                 "equals_device_result": fill_ok,
+                "default_call": {"path": "RoadRunnerModel(...).evaluate(numpy params) -> numpy float64 "
+                                         "(copy=True, the reference's signature and return type)",
+                                 "split_ms": dc_split * 1e3, "split_points_per_s": npv * npt / dc_split,
+                                 "fp64_ms": dc_fp64 * 1e3, "fp64_points_per_s": npv * npt / dc_fp64,
+                                 "d2h_bytes_per_call_fp64": npv * npt * 8},
                 "copy_path": {"value": world * npv * npt / e2e_copy_s, "ms_per_step": e2e_copy_s * 1e3,
                               "d2h_bytes_per_step": npv * npt * 4, "equals_device_result": copy_ok,
                               "path": "the same call with host_fill=False: the whole flux computed on the "

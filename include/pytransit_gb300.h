@@ -145,6 +145,16 @@ int rr_flux_f64(const double *times, int npt, const double *k, int nkc, const do
                 const double *istar, int ng, double dg, const void *workspace, double *flux, int ldflux,
                 void *stream);
 
+/* rr_flux_f64 for the parameter vectors [pv0, pv1) of the prepared
+ * workspace, into their own rows flux[pv1 - pv0, ldflux] (the arrays k, t0,
+ * p, istar are the whole population's).  Lets a caller copy the flux of one
+ * range to the host while the next is computed. */
+int rr_flux_f64_range(const double *times, int npt, const double *k, int nkc, const double *t0, int ldt0,
+                      const double *p, int npv, int nlc, int npb, const int32_t *lcids, const int32_t *pbids,
+                      const int32_t *epids, const int32_t *nsamples, const double *exptimes,
+                      const double *istar, int ng, double dg, const void *workspace, int pv0, int pv1,
+                      double *flux, int ldflux, void *stream);
+
 /* The two stages of rr_full_split: the prologue writes the per-parameter-vector
  * and per-(pv, light curve) tables into the workspace, the flux stage reads
  * only those tables, the FP32-pair times and the light-curve ids. */
@@ -203,6 +213,17 @@ int rr_flux_split_transits(const float *times_ff, int npt, const int32_t *lcids,
  * a process forked after that starts its own.  No GPU work.  Returns 0, or
  * RR_ERR_ARG for dst NULL with n > 0. */
 int rr_host_fill_f32(float *dst, size_t n, float value, int nthreads);
+int rr_host_fill_f64(double *dst, size_t n, double value, int nthreads);
+
+/* rr_flux_split_range and rr_flux_split_transits with FP64 output rows (the
+ * reference's output type, model_full.py:75): each FP32 result widened
+ * exactly, the same values as the FP32 rows. */
+int rr_flux_split_range_f64(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb,
+                            int ng, double dg, const void *workspace, int pv0, int pv1, double *flux, int ldflux,
+                            void *stream);
+int rr_flux_split_transits_f64(const float *times_ff, int npt, const int32_t *lcids, int npv, int nlc, int npb,
+                               int ng, double dg, const void *workspace, int pv0, int pv1, double *flux,
+                               int ldflux, void *stream);
 
 /* ---- transmission-spectroscopy model --------------------------------------- */
 

@@ -59,6 +59,11 @@ def _sig(L):
     L.rr_flux_split_range.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
     L.rr_flux_split_transits.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
     L.rr_host_fill_f32.argtypes = [_vp, _sz, C.c_float, _i]
+    L.rr_host_fill_f64.argtypes = [_vp, _sz, _d, _i]
+    L.rr_flux_split_range_f64.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
+    L.rr_flux_split_transits_f64.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
+    L.rr_flux_f64_range.argtypes = ([_vp, _i, _vp, _i, _vp, _i, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i,
+                                     _d, _vp, _i, _i, _vp, _i, _vp])
     L.rr_ts_workspace_bytes.argtypes = [_i, _i, _i, _i]
     L.rr_ts_workspace_bytes.restype = _sz
     _ts_tail = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _d,

@@ -613,8 +613,32 @@ struct FluxSplitArgs {
   const float *orb32, *lc32, *ldm;
   int npt, npv, npb, nlc, ng, ldflux;
   float inv_dg;
-  float* flux;
+  void* flux;          // float or double rows (the kernel's OutT)
   int transits_only;   // store only the tiles that reach a transit (and invalid rows); the rest holds 1
+};
+
+// Output rows of the split flux kernels: FP32 (the split path's own type), or
+// FP64 (the reference's output type, each FP32 result widened exactly).  A
+// culled tile is one 16-byte store of the fill value per lane (FP32) or two
+// (FP64).
+template <typename OutT>
+struct TileOut;
+
+template <>
+struct TileOut<float> {
+  static __device__ __forceinline__ void fill(float* row, int tile, int lane, float v) {
+    __stcs(reinterpret_cast<float4*>(row) + lane + (size_t)tile * (32 * 4 / 4), make_float4(v, v, v, v));
+  }
+};
+
+template <>
+struct TileOut<double> {
+  static __device__ __forceinline__ void fill(double* row, int tile, int lane, float v) {
+    const double d = v;
+    double2* q = reinterpret_cast<double2*>(row) + (size_t)tile * 64 + 2 * lane;
+    __stcs(q, make_double2(d, d));
+    __stcs(q + 1, make_double2(d, d));
+  }
 };
 
 constexpr int LC_SMEM = 64;                  // light-curve records staged in shared memory
@@ -928,6 +952,7 @@ __device__ __forceinline__ void split_tile_points(const float* __restrict__ orb,
 // the stores of the culled tiles (walking the set bits of the cull mask),
 // then the per-point path of the others.  Ends without a barrier: the caller
 // synchronises before staging another pv.
+template <typename OutT>
 __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, int t_first, int t_step, int t_end,
                                                float* recs, bool lc_in_smem, WarpList* lists) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -943,7 +968,7 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
   const bool wide = flags & FLAG_WIDE;
   const float p_hi = orb[10], inv_p = orb[12];
   const float* ldm_pv = A.ldm + (size_t)pv * A.npb * A.ng;
-  float* row = A.flux + (size_t)pv * A.ldflux;
+  OutT* row = static_cast<OutT*>(A.flux) + (size_t)pv * A.ldflux;
   const bool row_vec = ((A.ldflux & 3) == 0) && ((reinterpret_cast<uintptr_t>(A.flux) & 15) == 0);
   const float4* meta = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(A.times_ff) +
                                                        time_meta_offset(A.npt));
@@ -957,7 +982,6 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
   const int ntl = tw0 < t_end ? (t_end - tw0 + t_step - 1) / t_step : 0;
   const int tile_part = (A.npt % WARP_TILE) ? A.npt / WARP_TILE : -1;
   const float fill = valid ? 1.0f : __int_as_float(0x7fc00000);
-  const float4 fill4 = make_float4(fill, fill, fill, fill);
   for (int j0 = 0; j0 < ntl; j0 += 32) {
     // The cull test of the warp's next 32 tiles, one tile per lane: the
     // tile's time range (from its summary) against the box copies around it,
@@ -986,15 +1010,14 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
     const unsigned cmask = __ballot_sync(FULL, cull) & jmask;
     // the culled tiles first, walking the set bits of the mask (none when the
     // caller has already set the row to 1; an invalid pv's NaN always)
-    float4* const row4 = reinterpret_cast<float4*>(row) + lane;
     for (unsigned m = (A.transits_only && valid) ? 0u : cmask; m; m &= m - 1u) {
       const int tile = tw0 + (j0 + __ffs(m) - 1) * t_step;
       if (row_vec && tile != tile_part) {
-        __stcs(row4 + (size_t)tile * (WARP_TILE / 4), fill4);
+        TileOut<OutT>::fill(row, tile, lane, fill);
       } else {
         const int pt0 = tile * WARP_TILE + lane * SPLIT_PTS;
         for (int q = 0; q < SPLIT_PTS; ++q)
-          if (pt0 + q < A.npt) __stcs(row + pt0 + q, fill);
+          if (pt0 + q < A.npt) __stcs(row + pt0 + q, (OutT)fill);
       }
     }
     // then the tiles that reach a box copy
@@ -1021,7 +1044,7 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
       split_tile_points(orb, LCR, ldm_pv, A.ng, A.inv_dg, wide, tm, hi, lo, lcv, L, lane, res);
 #pragma unroll
       for (int q = 0; q < SPLIT_PTS; ++q)
-        if (ps0 + 32 * q < A.npt) __stcs(row + ps0 + 32 * q, res[q]);
+        if (ps0 + 32 * q < A.npt) __stcs(row + ps0 + 32 * q, (OutT)res[q]);
     }
   }
 }
@@ -1036,7 +1059,7 @@ __device__ __forceinline__ void split_pv_tiles(const FluxSplitArgs& A, int pv, i
 constexpr int FLUX_NW = 2;
 constexpr int FLUX_CHUNK = 32;
 
-template <bool LC_IN_SMEM>
+template <bool LC_IN_SMEM, typename OutT>
 __global__ void __launch_bounds__(FLUX_NW * 32) flux_split_kernel(FluxSplitArgs A, int chunk) {
   __shared__ WarpList lists[FLUX_NW];
   extern __shared__ __align__(16) float flux_recs[];
@@ -1045,7 +1068,7 @@ __global__ void __launch_bounds__(FLUX_NW * 32) flux_split_kernel(FluxSplitArgs 
   const int ntiles = (A.npt + WARP_TILE - 1) / WARP_TILE;
   const int t0 = blockIdx.x * chunk;
   const int t1 = t0 + chunk < ntiles ? t0 + chunk : ntiles;
-  split_pv_tiles(A, pv, t0, FLUX_NW, t1, flux_recs, LC_IN_SMEM, lists);
+  split_pv_tiles<OutT>(A, pv, t0, FLUX_NW, t1, flux_recs, LC_IN_SMEM, lists);
 }
 
 // ---------------------------------------------------------------------------
@@ -1099,7 +1122,7 @@ serve_split_kernel(const rr_serve_request* __restrict__ reqs, const rr_serve_ite
     A.inv_dg = r.inv_dg; A.flux = r.flux;
     const bool lc_smem = r.nlc <= LC_SMEM;
     for (int pv = w.pv0; pv < w.pv1; ++pv) {
-      split_pv_tiles(A, pv, w.tile0, SPLIT_WARPS, w.tile1, recs, lc_smem, lists);
+      split_pv_tiles<float>(A, pv, w.tile0, SPLIT_WARPS, w.tile1, recs, lc_smem, lists);
       __syncthreads();
     }
   }
@@ -1176,25 +1199,39 @@ int rr_prepare_f64(const double* k, int nkc, const double* p, const double* a, c
   return check_launch("rr_prepare_f64");
 }
 
+int rr_flux_f64_range(const double* times, int npt, const double* k, int nkc, const double* t0, int ldt0,
+                      const double* p, int npv, int nlc, int npb, const int32_t* lcids, const int32_t* pbids,
+                      const int32_t* epids, const int32_t* nsamples, const double* exptimes,
+                      const double* istar, int ng, double dg, const void* workspace, int pv0, int pv1,
+                      double* flux, int ldflux, void* stream) {
+  if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
+  if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || nkc < 1 || ldflux < npt) return RR_ERR_ARG;
+  if (pv0 < 0 || pv1 > npv || pv0 > pv1) return RR_ERR_ARG;
+  if (pv1 == pv0 || npt == 0) return RR_OK;
+  Carve cv(const_cast<void*>(workspace));
+  double* orb = cv.take<double>((size_t)npv * ORB64);
+  double* ldm = cv.take<double>((size_t)npv * npb * ng);
+  // the range's parameters and records: the kernel indexes pv from 0 within it
+  FluxF64Args fa{};
+  fa.times = times; fa.k = k + (size_t)pv0 * nkc; fa.t0 = t0 + (size_t)pv0 * ldt0; fa.p = p + pv0;
+  fa.exptimes = exptimes; fa.istar = istar + (size_t)pv0 * npb;
+  fa.ldm = ldm + (size_t)pv0 * npb * ng; fa.orb64 = orb + (size_t)pv0 * ORB64;
+  fa.lcids = lcids; fa.pbids = pbids; fa.epids = epids;
+  fa.nsamples = nsamples; fa.npt = npt; fa.npv = pv1 - pv0; fa.nkc = nkc; fa.ldt0 = ldt0; fa.npb = npb;
+  fa.ng = ng; fa.ldflux = ldflux; fa.dg = dg; fa.flux = flux;
+  const int n = pv1 - pv0;
+  dim3 fg((npt + 255) / 256, n < 65535 ? n : 65535, (n + 65534) / 65535);
+  flux_f64_kernel<<<fg, 256, 0, as_stream(stream)>>>(fa);
+  return check_launch("rr_flux_f64");
+}
+
 int rr_flux_f64(const double* times, int npt, const double* k, int nkc, const double* t0, int ldt0,
                 const double* p, int npv, int nlc, int npb, const int32_t* lcids, const int32_t* pbids,
                 const int32_t* epids, const int32_t* nsamples, const double* exptimes,
                 const double* istar, int ng, double dg, const void* workspace, double* flux, int ldflux,
                 void* stream) {
-  if (nkc > 1 && nkc != npb) return RR_ERR_SHAPE;
-  if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || nkc < 1 || ldflux < npt) return RR_ERR_ARG;
-  if (npv == 0 || npt == 0) return RR_OK;
-  Carve cv(const_cast<void*>(workspace));
-  double* orb = cv.take<double>((size_t)npv * ORB64);
-  double* ldm = cv.take<double>((size_t)npv * npb * ng);
-  FluxF64Args fa{};
-  fa.times = times; fa.k = k; fa.t0 = t0; fa.p = p; fa.exptimes = exptimes; fa.istar = istar;
-  fa.ldm = ldm; fa.orb64 = orb; fa.lcids = lcids; fa.pbids = pbids; fa.epids = epids;
-  fa.nsamples = nsamples; fa.npt = npt; fa.npv = npv; fa.nkc = nkc; fa.ldt0 = ldt0; fa.npb = npb;
-  fa.ng = ng; fa.ldflux = ldflux; fa.dg = dg; fa.flux = flux;
-  dim3 fg((npt + 255) / 256, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
-  flux_f64_kernel<<<fg, 256, 0, as_stream(stream)>>>(fa);
-  return check_launch("rr_flux_f64");
+  return rr_flux_f64_range(times, npt, k, nkc, t0, ldt0, p, npv, nlc, npb, lcids, pbids, epids, nsamples, exptimes,
+                           istar, ng, dg, workspace, 0, npv, flux, ldflux, stream);
 }
 
 int rr_full_f64(const double* times, int npt, const double* k, int nkc, const double* t0, int ldt0,
@@ -1302,8 +1339,8 @@ int rr_flux_split(const float* times_ff, int npt, const int32_t* lcids, int npv,
 }
 
 static int flux_split_launch(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb,
-                             int ng, double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
-                             void* stream, int transits_only) {
+                             int ng, double dg, const void* workspace, int pv0, int pv1, void* flux, int ldflux,
+                             void* stream, int transits_only, bool out_f64) {
   if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || ldflux < npt) return RR_ERR_ARG;
   if (pv0 < 0 || pv1 > npv || pv0 > pv1) return RR_ERR_ARG;
   if (pv1 == pv0 || npt == 0) return RR_OK;
@@ -1328,39 +1365,76 @@ static int flux_split_launch(const float* times_ff, int npt, const int32_t* lcid
   const bool lc_smem = nlc <= LC_SMEM;
   const size_t smem = sizeof(float) * (ORB32 + (lc_smem ? (size_t)nlc * LC32 : 0));
   cudaStream_t s = as_stream(stream);
-  if (lc_smem)
-    flux_split_kernel<true><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
-  else
-    flux_split_kernel<false><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
+  if (out_f64) {
+    if (lc_smem)
+      flux_split_kernel<true, double><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
+    else
+      flux_split_kernel<false, double><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
+  } else {
+    if (lc_smem)
+      flux_split_kernel<true, float><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
+    else
+      flux_split_kernel<false, float><<<fg, FLUX_NW * 32, smem, s>>>(fa, (int)chunk);
+  }
   return check_launch("rr_flux_split");
+}
+
+// The device address of output rows given as device memory or page-locked
+// host memory; NULL for anything else (pageable host memory).
+static void* device_rows(void* flux, int* status) {
+  *status = RR_OK;
+  if (!flux) {
+    *status = RR_ERR_ARG;
+    return nullptr;
+  }
+  cudaPointerAttributes at{};
+  const cudaError_t e = cudaPointerGetAttributes(&at, flux);
+  if (e != cudaSuccess) {
+    set_cuda_error(e, "rr_flux_split_transits (pointer)");
+    *status = RR_ERR_CUDA;
+    return nullptr;
+  }
+  void* dst = nullptr;
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)
+    dst = flux;
+  else if (at.type == cudaMemoryTypeHost)
+    dst = at.devicePointer;
+  if (!dst) *status = RR_ERR_ARG;   // pageable host memory: not reachable by the kernel here
+  return dst;
 }
 
 int rr_flux_split_range(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
                         double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
                         void* stream) {
   return flux_split_launch(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, pv0, pv1, flux, ldflux, stream,
-                           0);
+                           0, false);
+}
+
+int rr_flux_split_range_f64(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb,
+                            int ng, double dg, const void* workspace, int pv0, int pv1, double* flux, int ldflux,
+                            void* stream) {
+  return flux_split_launch(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, pv0, pv1, flux, ldflux, stream,
+                           0, true);
 }
 
 int rr_flux_split_transits(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
                            double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
                            void* stream) {
-  if (!flux) return RR_ERR_ARG;
-  // page-locked host rows are written through their device address
-  cudaPointerAttributes at{};
-  const cudaError_t e = cudaPointerGetAttributes(&at, flux);
-  if (e != cudaSuccess) {
-    set_cuda_error(e, "rr_flux_split_transits (pointer)");
-    return RR_ERR_CUDA;
-  }
-  float* dst = nullptr;
-  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)
-    dst = flux;
-  else if (at.type == cudaMemoryTypeHost)
-    dst = static_cast<float*>(at.devicePointer);
-  if (!dst) return RR_ERR_ARG;   // pageable host memory: not reachable by the kernel here
+  int st;
+  void* dst = device_rows(flux, &st);
+  if (!dst) return st;
   return flux_split_launch(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, pv0, pv1, dst, ldflux, stream,
-                           1);
+                           1, false);
+}
+
+int rr_flux_split_transits_f64(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb,
+                               int ng, double dg, const void* workspace, int pv0, int pv1, double* flux,
+                               int ldflux, void* stream) {
+  int st;
+  void* dst = device_rows(flux, &st);
+  if (!dst) return st;
+  return flux_split_launch(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, pv0, pv1, dst, ldflux, stream,
+                           1, true);
 }
 
 int rr_full_split(const float* times_ff, double t_ref, double t_absmax, int npt, const double* k, int nkc,

@@ -30,35 +30,46 @@ struct FillPool {
   unsigned long long generation = 0;
   int workers = 0;
   int remaining = 0;
-  float* dst = nullptr;
+  void* dst = nullptr;
   size_t n = 0;
-  float value = 0.0f;
+  double value = 0.0;
+  bool f64 = false;
   int parts = 1;
   pid_t owner = 0;
 
-  static void fill_slice(float* dst, size_t n, float value, int parts, int part) {
-    // slices are whole 16-float (64-byte) blocks except the last
-    const size_t blocks = (n + 15) / 16;
+  template <typename T>
+  static void fill_slice_t(T* dst, size_t n, T value, int parts, int part) {
+    // slices are whole 64-byte blocks except the last
+    constexpr size_t B = 64 / sizeof(T);
+    const size_t blocks = (n + B - 1) / B;
     const size_t per = (blocks + parts - 1) / parts;
     const size_t b0 = std::min(blocks, per * (size_t)part), b1 = std::min(blocks, b0 + per);
-    const size_t i0 = b0 * 16, i1 = std::min(n, b1 * 16);
-    float* p = dst + i0;
+    const size_t i0 = b0 * B, i1 = std::min(n, b1 * B);
+    T* p = dst + i0;
     for (size_t i = i0; i < i1; ++i) *p++ = value;
+  }
+
+  static void fill_slice(void* dst, size_t n, double value, bool f64, int parts, int part) {
+    if (f64)
+      fill_slice_t<double>(static_cast<double*>(dst), n, value, parts, part);
+    else
+      fill_slice_t<float>(static_cast<float*>(dst), n, (float)value, parts, part);
   }
 
   void worker(int id, unsigned long long seen) {
     for (;;) {
-      float* d;
+      void* d;
       size_t nn;
-      float v;
+      double v;
+      bool dbl;
       int np;
       {
         std::unique_lock<std::mutex> lk(m);
         go.wait(lk, [&] { return generation != seen; });
         seen = generation;
-        d = dst; nn = n; v = value; np = parts;
+        d = dst; nn = n; v = value; dbl = f64; np = parts;
       }
-      if (id < np - 1) fill_slice(d, nn, v, np, id);
+      if (id < np - 1) fill_slice(d, nn, v, dbl, np, id);
       std::lock_guard<std::mutex> lk(m);
       if (--remaining == 0) done.notify_one();
     }
@@ -74,22 +85,22 @@ struct FillPool {
     }
   }
 
-  void run(float* d, size_t nn, float v, int nthreads) {
+  void run(void* d, size_t nn, double v, bool dbl, int nthreads) {
     std::lock_guard<std::mutex> serial(call);
     const int np = std::max(1, nthreads);
     if (np > 1) ensure(np - 1);
     if (np == 1) {
-      fill_slice(d, nn, v, 1, 0);
+      fill_slice(d, nn, v, dbl, 1, 0);
       return;
     }
     {
       std::lock_guard<std::mutex> lk(m);
-      dst = d; n = nn; value = v; parts = np;
+      dst = d; n = nn; value = v; f64 = dbl; parts = np;
       remaining = workers;   // every worker wakes and reports, busy or not
       ++generation;
     }
     go.notify_all();
-    fill_slice(d, nn, v, np, np - 1);
+    fill_slice(d, nn, v, dbl, np, np - 1);
     std::unique_lock<std::mutex> lk(m);
     done.wait(lk, [&] { return remaining == 0; });
   }
@@ -112,12 +123,20 @@ FillPool* pool() {
 
 }  // namespace
 
-extern "C" int rr_host_fill_f32(float* dst, size_t n, float value, int nthreads) {
+static int host_fill(void* dst, size_t n, double value, bool f64, int nthreads) {
   if (n == 0) return RR_OK;
   if (!dst) return RR_ERR_ARG;
   if (nthreads > 256) nthreads = 256;
   // small fills are not worth a wake-up of the pool
   if (n < ((size_t)1 << 16)) nthreads = 1;
-  pool()->run(dst, n, value, nthreads);
+  pool()->run(dst, n, value, f64, nthreads);
   return RR_OK;
+}
+
+extern "C" int rr_host_fill_f32(float* dst, size_t n, float value, int nthreads) {
+  return host_fill(dst, n, value, false, nthreads);
+}
+
+extern "C" int rr_host_fill_f64(double* dst, size_t n, double value, int nthreads) {
+  return host_fill(dst, n, value, true, nthreads);
 }

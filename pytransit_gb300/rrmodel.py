@@ -355,32 +355,44 @@ class RoadRunnerModel(TransitModel):
         comp.wait_stream(cs)
         return 0
 
-    def _flux_to_pinned(self, dd, npt, npv, nlc, npb, ws, out2d, device, nchunks=4):
-        """Split-path flux into the pinned host rows out2d[npv, npt] over the
-        host link and the host's own memory bandwidth at once.  The first
-        rows (a 1 - host_fill_fraction share) are computed on the device in
-        one launch and copied over on a copy stream.  Meanwhile the host sets
-        the other rows to 1, a pv chunk at a time, on the library's threads
-        (rr_host_fill_f32), and after each chunk the GPU writes that chunk's
-        transit tiles and invalid rows straight into it
-        (rr_flux_split_transits): tiles that reach no transit window never
-        cross the link.  The current stream waits for the copy; the caller
-        synchronises it.  Returns the first non-zero status."""
+    # copy=True results of at least this many points are written straight
+    # into pinned host memory (torch's cached host allocator), smaller ones
+    # copied from the device
+    PINNED_RESULT_MIN = 1 << 17
+
+    def _flux_to_pinned(self, dd, npt, npv, nlc, npb, ws, out2d, device, nchunks=4, fill_fraction=None):
+        """Split-path flux into the pinned host rows out2d[npv, npt] (float32,
+        or float64 with each FP32 result widened) over the host link and the
+        host's own memory bandwidth at once.  The first rows (a
+        1 - host_fill_fraction share) are computed on the device in one launch
+        and copied over on a copy stream.  Meanwhile the host sets the other
+        rows to 1, a pv chunk at a time, on the library's threads
+        (rr_host_fill_f32/_f64), and after each chunk the GPU writes that
+        chunk's transit tiles and invalid rows straight into it
+        (rr_flux_split_transits[_f64]): tiles that reach no transit window
+        never cross the link.  The current stream waits for the copy; the
+        caller synchronises it.  Returns the first non-zero status."""
         import torch
         from . import _lib
         L, P = _lib.lib(), _lib.ptr
+        f64 = out2d.dtype == torch.float64
+        esize = 8 if f64 else 4
+        dense = L.rr_flux_split_range_f64 if f64 else L.rr_flux_split_range
+        transits = L.rr_flux_split_transits_f64 if f64 else L.rr_flux_split_transits
+        fill = L.rr_host_fill_f64 if f64 else L.rr_host_fill_f32
         comp = torch.cuda.current_stream(device)
         sp = C.c_void_p(comp.cuda_stream)
-        ncopy = int(round(npv * (1.0 - min(1.0, max(0.0, float(self.host_fill_fraction))))))
+        frac = self.host_fill_fraction if fill_fraction is None else fill_fraction
+        ncopy = int(round(npv * (1.0 - min(1.0, max(0.0, float(frac))))))
         cs = None
         if ncopy > 0:
-            key = (device, ncopy, npt)
+            key = (device, ncopy, npt, out2d.dtype)
             if getattr(self, '_stage', None) is None or self._stage[0] != key:
-                self._stage = (key, torch.empty((ncopy, npt), dtype=torch.float32, device=device),
+                self._stage = (key, torch.empty((ncopy, npt), dtype=out2d.dtype, device=device),
                                torch.cuda.Stream(device))
             _, buf, cs = self._stage
-            st = L.rr_flux_split_range(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg,
-                                       P(ws), 0, ncopy, P(buf), npt, sp)
+            st = dense(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg, P(ws), 0, ncopy,
+                       P(buf), npt, sp)
             if st != 0:
                 return st
             cs.wait_stream(comp)
@@ -391,15 +403,54 @@ class RoadRunnerModel(TransitModel):
         bounds = ncopy + np.linspace(0, nfill, min(nchunks, nfill) + 1).astype(int) if nfill > 0 else []
         for c in range(len(bounds) - 1):
             pv0, pv1 = int(bounds[c]), int(bounds[c + 1])
-            rows = C.c_void_p(base + pv0 * npt * 4)
-            st = L.rr_host_fill_f32(rows, (pv1 - pv0) * npt, 1.0, int(self.host_threads))
+            rows = C.c_void_p(base + pv0 * npt * esize)
+            st = fill(rows, (pv1 - pv0) * npt, 1.0, int(self.host_threads))
             if st == 0:
-                st = L.rr_flux_split_transits(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng,
-                                              self.dg, P(ws), pv0, pv1, rows, npt, sp)
+                st = transits(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg, P(ws),
+                              pv0, pv1, rows, npt, sp)
             if st != 0:
                 return st
         if cs is not None:
             comp.wait_stream(cs)
+        return 0
+
+    def _flux64_to_host(self, args, dd, istar, npt, npv, nlc, npb, ws, out2d, device, nchunks=8):
+        """Plain FP64 flux into the pinned host rows out2d[npv, npt]: the pv
+        range in chunks (rr_flux_f64_range) through two device buffers, each
+        chunk copied to the host on a copy stream while the next one is
+        computed.  Returns the first non-zero status."""
+        import torch
+        from . import _lib
+        L, P = _lib.lib(), _lib.ptr
+        bounds = np.linspace(0, npv, min(nchunks, npv) + 1).astype(int)
+        rows = int(np.diff(bounds).max())
+        key = (device, rows, npt)
+        if getattr(self, '_pipe64', None) is None or self._pipe64[0] != key:
+            self._pipe64 = (key, [torch.empty((rows, npt), dtype=torch.float64, device=device) for _ in range(2)],
+                            torch.cuda.Stream(device))
+        _, bufs, cs = self._pipe64
+        comp = torch.cuda.current_stream(device)
+        sp = C.c_void_p(comp.cuda_stream)
+        k, t0 = args['k'], args['t0']
+        copied = [None, None]
+        for c in range(len(bounds) - 1):
+            pv0, pv1 = int(bounds[c]), int(bounds[c + 1])
+            b = bufs[c % 2]
+            if copied[c % 2] is not None:
+                comp.wait_event(copied[c % 2])
+            st = L.rr_flux_f64_range(P(dd['time']), npt, P(k), k.shape[1], P(t0), t0.shape[1], P(args['p']), npv,
+                                     nlc, npb, P(dd['lcids']), P(dd['pbids']), P(dd['epids']), P(dd['nsamples']),
+                                     P(dd['exptimes']), P(istar), self.ng, self.dg, P(ws), pv0, pv1, P(b), npt, sp)
+            if st != 0:
+                return st
+            done = torch.cuda.Event()
+            done.record(comp)
+            cs.wait_event(done)
+            with torch.cuda.stream(cs):
+                out2d[pv0:pv1].copy_(b[:pv1 - pv0], non_blocking=True)
+                copied[c % 2] = torch.cuda.Event()
+                copied[c % 2].record(cs)
+        comp.wait_stream(cs)
         return 0
 
     def evaluate(self, k: Union[float, ndarray], ldc: Union[ndarray, List], t0: Union[float, ndarray],
@@ -410,15 +461,21 @@ class RoadRunnerModel(TransitModel):
 
         Returns the modelled flux, [npt] for one parameter vector and
         [npv, npt] for many (squeezed as the reference does).  With copy=True a
-        float64 numpy array; with copy=False the torch tensor on the GPU
-        (float64, or float32 in the split precision).  ``out``: an optional
-        [npv, npt] torch tensor (pinned host memory or device) that receives the
-        flux; it is filled, synchronised and returned.  In the split path a
-        contiguous pinned host float32 tensor is filled in parameter-vector
-        chunks: the host sets a chunk's rows to 1 (``host_threads`` threads)
-        while the GPU writes the tiles of the chunk before it that reach a
-        transit window straight into that memory, so the out-of-transit
-        points never cross the host link.
+        float64 numpy array; from PINNED_RESULT_MIN points on it is a view of
+        page-locked host memory from torch's cached host allocator, which the
+        GPU fills directly.  With copy=False the torch tensor on the GPU
+        (float64, or float32 in the split precision).
+
+        ``out``: an optional [npv, npt] torch tensor (pinned host memory or
+        device) that receives the flux; it is filled, synchronised and
+        returned.  Contiguous pinned host rows (float32 or float64 in the split
+        path, float64 in the plain one) are filled without a device copy of
+        the whole result.  In the split path part of the rows are computed on
+        the device and copied over, while the host sets the others to 1
+        (``host_threads`` threads) and the GPU writes their tiles that reach a
+        transit window straight into them, so out-of-transit points need not
+        cross the host link.  The plain path copies pv chunks over while the
+        next chunk is computed.
 
         return_error=True returns (flux, bound): the stated maximum absolute
         flux error of this result against the FP64 model (see
@@ -503,11 +560,19 @@ class RoadRunnerModel(TransitModel):
         else:
             ldp, istar = self._ld_tables(ldc, npv, npb, device, split, ldc_d)
         kmin, kmax = float(self.klims[0]), float(self.klims[1])
-        # A pinned host float32 buffer for the split path is filled in pv
-        # chunks: chunk c+1 is computed while chunk c is copied to the host.
-        pipe = (split and user_out is not None and user_out.device.type == 'cpu' and user_out.is_pinned()
-                and user_out.is_contiguous() and user_out.numel() == npv * npt and user_out.dtype == torch.float32
-                and npv >= 2)
+        # Host rows the flux goes to directly: a caller's contiguous pinned
+        # buffer (float32 or float64 in the split path, float64 in the plain
+        # one), or, for copy=True, a pinned float64 buffer from torch's cached
+        # host allocator whose numpy view is returned.
+        host_rows = None
+        if user_out is not None:
+            if (user_out.device.type == 'cpu' and user_out.is_pinned() and user_out.is_contiguous()
+                    and user_out.numel() == npv * npt
+                    and user_out.dtype in ((torch.float32, torch.float64) if split else (torch.float64,))):
+                host_rows = user_out.view(npv, npt)
+        elif copy and npv * npt >= self.PINNED_RESULT_MIN:
+            host_rows = torch.empty((npv, npt), dtype=torch.float64, pin_memory=True)
+        pipe = host_rows is not None
         if split:
             ldf = (npt + 3) // 4 * 4
             res = None if pipe else torch.empty((npv, ldf), dtype=torch.float32, device=device)
@@ -530,21 +595,27 @@ class RoadRunnerModel(TransitModel):
                                         self.nk, self.ng, nz, self.dk, kmin, kmax, P(tb['ze']), P(ws), ws.numel(),
                                         stream, self.ld_law or 0, P(ldc_d), npar, P(basis), nb)
             if st == 0 and pipe:
-                to_host = self._flux_to_pinned if self.host_fill else self._flux_to_host
-                st = to_host(dd, npt, npv, nlc, npb, ws, user_out.view(npv, npt), device)
+                if self.host_fill:
+                    st = self._flux_to_pinned(dd, npt, npv, nlc, npb, ws, host_rows, device)
+                elif host_rows.dtype == torch.float32:
+                    st = self._flux_to_host(dd, npt, npv, nlc, npb, ws, host_rows, device)
+                else:
+                    st = self._flux_to_pinned(dd, npt, npv, nlc, npb, ws, host_rows, device, fill_fraction=0.0)
             elif st == 0:
                 st = L.rr_flux_split(P(dd['times_ff']), npt, P(dd['lcids']), npv, nlc, npb, self.ng, self.dg,
                                      P(ws), P(res), ldf, stream)
             res = None if pipe else res[:, :npt]
         else:
-            res = torch.empty((npv, npt), dtype=torch.float64, device=device)
+            res = None if pipe else torch.empty((npv, npt), dtype=torch.float64, device=device)
             wsb = L.rr_full_f64_workspace_bytes(npv, npb, self.ng)
             ws = self._workspace(wsb, device)
             st = L.rr_prepare_f64(P(args['k']), k.shape[1], P(args['p']), P(args['a']), P(args['i']),
                                   P(args['e']), P(args['w']), npv, npb, P(ldp), P(tb['W64']), self.nk, self.ng, nz,
                                   self.dk, kmin, kmax, P(tb['ze']), P(ws), ws.numel(), stream,
                                   self.ld_law or 0, P(ldc_d), npar, P(basis), nb)
-            if st == 0:
+            if st == 0 and pipe:
+                st = self._flux64_to_host(args, dd, istar, npt, npv, nlc, npb, ws, host_rows, device)
+            elif st == 0:
                 st = L.rr_flux_f64(P(dd['time']), npt, P(args['k']), k.shape[1], P(args['t0']), t0.shape[1],
                                    P(args['p']), npv, nlc, npb, P(dd['lcids']), P(dd['pbids']), P(dd['epids']),
                                    P(dd['nsamples']), P(dd['exptimes']), P(istar), self.ng, self.dg, P(ws),
@@ -552,10 +623,12 @@ class RoadRunnerModel(TransitModel):
         _lib.check(st, "rr_full")
         self._bound_state = dict(split=split, npv=npv, npb=npb, nlc=nlc, nep=t0.shape[1], ws=ws, device=device,
                                  prm={n: args[n] for n in ('p', 'a', 'i', 'e', 'w')})
+        if pipe:
+            torch.cuda.current_stream(device).synchronize()
+            return user_out if user_out is not None else host_rows.numpy().squeeze()
         if user_out is not None:
-            if not pipe:
-                src = res if user_out.dtype == res.dtype else res.to(user_out.dtype)
-                user_out.view(npv, npt).copy_(src, non_blocking=True)
+            src = res if user_out.dtype == res.dtype else res.to(user_out.dtype)
+            user_out.view(npv, npt).copy_(src, non_blocking=True)
             torch.cuda.current_stream(device).synchronize()
             return user_out
         res = res.squeeze()

@@ -325,3 +325,45 @@ def test_flux_split_transits_writes_only_transit_tiles():
     pageable = np.ones((npv, npt), np.float32)
     assert L.rr_flux_split_transits(P(dd['times_ff']), npt, P(dd['lcids']), npv, st['nlc'], st['npb'], m.ng,
                                     m.dg, P(st['ws']), 0, npv, C.c_void_p(pageable.ctypes.data), npt, sp) == 2
+
+
+@pytest.mark.parametrize("precision,host_fill", [("fp64", True), ("split", True), ("split", False)])
+@pytest.mark.parametrize("npv", [1, 37])
+def test_copy_true_through_pinned_rows(precision, host_fill, npv):
+    """evaluate() with copy=True (the reference's default) on an output large
+    enough to go straight into pinned host rows: a float64 numpy array with
+    the same bits as the device result widened, squeezed as the reference
+    squeezes, NaN rows for invalid vectors; and out= a pinned float64 tensor
+    likewise.  The split path's float64 rows come from the FP64-output
+    kernels (rr_flux_split_range_f64 / rr_flux_split_transits_f64), the
+    plain path's from rr_flux_f64_range in chunks."""
+    import torch
+    rng = np.random.default_rng(5 + npv)
+    T = 2459000.0
+    npt = 150_001 if npv == 1 else 5003
+    time = T + np.linspace(-3.0, 3.0, npt)
+    a = rng.uniform(5, 9, npv)
+    if npv > 1:
+        a[[3, 20]] = 0.9
+    args = (rng.uniform(0.08, 0.12, (npv, 1)), [0.3, 0.1], T + rng.normal(0, 1e-3, (npv, 1)),
+            rng.uniform(1, 3, npv), a, np.full(npv, 1.54), 0.0, 0.0)
+    m = rr(precision=precision)
+    m.host_fill = host_fill
+    m.set_data(time)
+    assert npv * npt >= m.PINNED_RESULT_MIN
+    want = m.evaluate(*args, copy=False).double().cpu().numpy()
+    got = m.evaluate(*args)
+    assert isinstance(got, np.ndarray) and got.dtype == np.float64 and got.shape == want.shape
+    np.testing.assert_array_equal(got, want)
+    if npv > 1:
+        assert np.isnan(got[3]).all() and np.isnan(got[20]).all() and np.isfinite(got[0]).all()
+    again = m.evaluate(*args)          # a second result does not overwrite the first
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(again, want)
+    out = torch.full((npv, npt), -7.0, dtype=torch.float64, pin_memory=True)
+    assert m.evaluate(*args, out=out) is out
+    np.testing.assert_array_equal(out.numpy().reshape(want.shape), want)
+    # against the oracle, as every parity test
+    ref = oracle.OracleRoadRunner('quadratic')
+    ref.set_data(time)
+    assert max_err(got, ref.evaluate(*args)) <= TOL[precision]
