@@ -116,6 +116,20 @@ def check(status: int, where: str = ""):
         raise RRError(f"{where}: {msg}" if where else msg)
 
 
+def to_host_f64(t, min_points: int = 1 << 17):
+    """A device result as a float64 numpy array, the reference's return type.
+    From min_points on, the copy goes into page-locked memory from torch's
+    cached host allocator (the array is a view of it): a copy into a fresh
+    pageable numpy array runs at a fraction of the host link's speed."""
+    if t.numel() < min_points:
+        return t.to(torch.float64).cpu().numpy()
+    src = t.to(torch.float64).contiguous()
+    host = torch.empty(src.shape, dtype=torch.float64, pin_memory=True)
+    host.copy_(src, non_blocking=True)
+    torch.cuda.current_stream(t.device).synchronize()
+    return host.numpy()
+
+
 def require_cuda(device=None) -> torch.device:
     if not torch.cuda.is_available():
         raise RuntimeError("pytransit_gb300 needs a CUDA device (GB300, sm_103a); no CPU fallback exists")

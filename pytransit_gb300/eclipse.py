@@ -114,7 +114,7 @@ class EclipseModel(_GpuEclipseBase):
                                         wsb, P(out), self.npt, _lib.stream_ptr(dev)), "rr_eclipse_f64")
         if not copy:
             return out
-        return np.squeeze(out.cpu().numpy().astype(np.float64, copy=False))
+        return np.squeeze(_lib.to_host_f64(out))
 
     def __call__(self, *args, **kwargs):
         return self.evaluate(*args, **kwargs)
@@ -163,7 +163,7 @@ class EclipseSpectroscopyModel(_GpuEclipseBase):
             _lib.check(L.rr_es_f64(P(dd['time']), self.npt, P(g['k']), P(g['t0']), P(g['p']), P(g['a']), P(g['i']),
                                    P(g['e']), P(g['w']), P(g['rstar']), P(g['f']), npv, npb, ns0, ex0, P(ws), wsb,
                                    P(out), self.npt, _lib.stream_ptr(dev)), "rr_es_f64")
-        return out.cpu().numpy().astype(np.float64, copy=False) if copy else out
+        return _lib.to_host_f64(out) if copy else out
 
     def __call__(self, *args, **kwargs):
         return self.evaluate(*args, **kwargs)

@@ -106,7 +106,7 @@ class TransmissionSpectroscopyModel(RoadRunnerModel):
         self._bound_state = dict(split=split, ts=True, npv=npv, npb=npb, ns0=ns0, ex0=ex0, ws=ws, device=device,
                                  prm={n: args[n] for n in ('p', 'a', 'i', 'e', 'w')})
         if copy:
-            out = out.to(torch.float64).cpu().numpy()
+            out = _lib.to_host_f64(out)
         return (out, self.last_error_bound) if return_error else out
 
     def _host_ld(self, ldc3, npv, npb, device, dt):
