@@ -767,7 +767,8 @@ def bench_serve(args):
     import torch
     device = torch.device("cuda", 0)
     torch.cuda.set_device(device)
-    res = serve_suite(torch, device, rate=args.rate, duration_s=args.serve_s, plain_sample=args.plain_sample)
+    res = serve_suite(torch, device, rate=args.rate, duration_s=args.serve_s, plain_sample=args.plain_sample,
+                      max_probes=args.probes)
     line = {"metric": "served model points/s (Poisson request stream); p50/p99 latency",
             "value": res["points_per_s"], "unit": "model points/s", "n_gpus": 1, "higher_is_better": True,
             "data": "synthetic (seeded)", "config": {"workload": res["workload"]}, **res}
@@ -794,6 +795,8 @@ def main():
     ap.add_argument("--serve-s", type=float, default=5.0, help="serving leg: seconds of arrivals at --rate")
     ap.add_argument("--plain-sample", type=int, default=200,
                     help="serving leg: requests run one at a time through the plain FP64 path")
+    ap.add_argument("--probes", type=int, default=3,
+                    help="serving leg: runs at other rates that bracket the highest sustained rate")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -1061,7 +1064,7 @@ def main():
         del flux64, flux32, ws32, ws64
         torch.cuda.empty_cache()
         line["serve"] = serve_suite(torch, device, rate=args.rate, duration_s=args.serve_s,
-                                    plain_sample=args.plain_sample)
+                                    plain_sample=args.plain_sample, max_probes=args.probes)
     keep = {}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_baseline(data, prm, keep=keep)
