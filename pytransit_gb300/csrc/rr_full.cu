@@ -1338,11 +1338,17 @@ int rr_flux_split(const float* times_ff, int npt, const int32_t* lcids, int npv,
   return rr_flux_split_range(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, 0, npv, flux, ldflux, stream);
 }
 
+static int flux_split_args(int npt, int npv, int nlc, int npb, int ng, int pv0, int pv1, int ldflux) {
+  if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || ldflux < npt) return RR_ERR_ARG;
+  if (pv0 < 0 || pv1 > npv || pv0 > pv1) return RR_ERR_ARG;
+  return RR_OK;
+}
+
 static int flux_split_launch(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb,
                              int ng, double dg, const void* workspace, int pv0, int pv1, void* flux, int ldflux,
                              void* stream, int transits_only, bool out_f64) {
-  if (npt < 0 || npv < 0 || nlc < 1 || npb < 1 || ng < 2 || ldflux < npt) return RR_ERR_ARG;
-  if (pv0 < 0 || pv1 > npv || pv0 > pv1) return RR_ERR_ARG;
+  const int st = flux_split_args(npt, npv, nlc, npb, ng, pv0, pv1, ldflux);
+  if (st != RR_OK) return st;
   if (pv1 == pv0 || npt == 0) return RR_OK;
   SplitTables t = carve_split(const_cast<void*>(workspace), npv, npb, nlc, ng);
   FluxSplitArgs fa{};
@@ -1420,7 +1426,8 @@ int rr_flux_split_range_f64(const float* times_ff, int npt, const int32_t* lcids
 int rr_flux_split_transits(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb, int ng,
                            double dg, const void* workspace, int pv0, int pv1, float* flux, int ldflux,
                            void* stream) {
-  int st;
+  int st = flux_split_args(npt, npv, nlc, npb, ng, pv0, pv1, ldflux);
+  if (st != RR_OK || pv1 == pv0 || npt == 0) return st;
   void* dst = device_rows(flux, &st);
   if (!dst) return st;
   return flux_split_launch(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, pv0, pv1, dst, ldflux, stream,
@@ -1430,7 +1437,8 @@ int rr_flux_split_transits(const float* times_ff, int npt, const int32_t* lcids,
 int rr_flux_split_transits_f64(const float* times_ff, int npt, const int32_t* lcids, int npv, int nlc, int npb,
                                int ng, double dg, const void* workspace, int pv0, int pv1, double* flux,
                                int ldflux, void* stream) {
-  int st;
+  int st = flux_split_args(npt, npv, nlc, npb, ng, pv0, pv1, ldflux);
+  if (st != RR_OK || pv1 == pv0 || npt == 0) return st;
   void* dst = device_rows(flux, &st);
   if (!dst) return st;
   return flux_split_launch(times_ff, npt, lcids, npv, nlc, npb, ng, dg, workspace, pv0, pv1, dst, ldflux, stream,

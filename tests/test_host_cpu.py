@@ -69,6 +69,20 @@ def test_argument_errors_without_gpu():
     assert prepare_ld(2, 3, 4, big) == 1          # k with 3 columns and 4 passbands
     assert prepare_ld(2, 1, 4, 64) == 3           # workspace too small
     assert prepare_ld(99, 1, 4, big) == 5         # unknown law: the two-stage path's check
+    # the range and pinned-output flux entry points: bad ranges and row strides
+    # are refused before any pointer is looked at; an empty range does nothing
+    for fn in (L.rr_flux_split_range, L.rr_flux_split_range_f64, L.rr_flux_split_transits,
+               L.rr_flux_split_transits_f64):
+        assert fn(dev, 100, dev, 8, 1, 1, 100, 0.01, dev, 0, 9, dev, 100, None) == 2    # pv1 > npv
+        assert fn(dev, 100, dev, 8, 1, 1, 100, 0.01, dev, 5, 4, dev, 100, None) == 2    # pv0 > pv1
+        assert fn(dev, 100, dev, 8, 1, 1, 100, 0.01, dev, 0, 8, dev, 99, None) == 2     # ldflux < npt
+        assert fn(dev, 100, dev, 8, 1, 1, 100, 0.01, dev, 3, 3, dev, 100, None) == 0    # empty range
+    st = L.rr_flux_f64_range(dev, 100, dev, 1, dev, 1, dev, 8, 1, 1, dev, dev, dev, dev, dev, dev, 100, 0.01, dev,
+                             0, 9, dev, 100, None)
+    assert st == 2
+    st = L.rr_flux_f64_range(dev, 100, dev, 3, dev, 1, dev, 8, 1, 4, dev, dev, dev, dev, dev, dev, 100, 0.01, dev,
+                             0, 8, dev, 100, None)
+    assert st == 1                                # k with 3 columns and 4 passbands
 
 
 def test_z_grid_matches_oracle():
