@@ -145,6 +145,26 @@ int rr_flux_f64(const double *times, int npt, const double *k, int nkc, const do
                 const double *istar, int ng, double dg, const void *workspace, double *flux, int ldflux,
                 void *stream);
 
+/* FP64 summaries of the 128-point time tiles, for rr_flux_f64_culled_range:
+ * tiles64[4 * tile + 0..3] = (earliest time, latest time, light curve or -1
+ * when the tile holds several, 0); rr_time_tiles_f64_doubles(npt) doubles.
+ * Made once per data set, as rr_time_split (transitmodel.py:56-125). */
+size_t rr_time_tiles_f64_doubles(int npt);
+int rr_time_tiles_f64(const double *times, const int32_t *lcids, int npt, double *tiles64, void *stream);
+
+/* rr_flux_f64_range with the fold (model_full.py:88-91) done once per tile
+ * for the tiles that reach no box.  The reference's epoch and tc are
+ * non-decreasing in t with its own rounding, so a one-light-curve tile with
+ * the same epoch at both ends, whose two ends' tc miss the box, holds 1.0 at
+ * every point: the same bits as rr_flux_f64, for a fraction of its FP64
+ * work.  The other tiles take the per-point arithmetic of rr_flux_f64. */
+int rr_flux_f64_culled_range(const double *times, const double *tiles64, int npt, const double *k, int nkc,
+                             const double *t0, int ldt0, const double *p, int npv, int nlc, int npb,
+                             const int32_t *lcids, const int32_t *pbids, const int32_t *epids,
+                             const int32_t *nsamples, const double *exptimes, const double *istar, int ng,
+                             double dg, const void *workspace, int pv0, int pv1, double *flux, int ldflux,
+                             void *stream);
+
 /* rr_flux_f64 for the parameter vectors [pv0, pv1) of the prepared
  * workspace, into their own rows flux[pv1 - pv0, ldflux] (the arrays k, t0,
  * p, istar are the whole population's).  Lets a caller copy the flux of one

@@ -62,6 +62,11 @@ def _sig(L):
     L.rr_host_fill_f64.argtypes = [_vp, _sz, _d, _i]
     L.rr_flux_split_range_f64.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
     L.rr_flux_split_transits_f64.argtypes = [_vp, _i, _vp, _i, _i, _i, _i, _d, _vp, _i, _i, _vp, _i, _vp]
+    L.rr_time_tiles_f64_doubles.argtypes = [_i]
+    L.rr_time_tiles_f64_doubles.restype = _sz
+    L.rr_time_tiles_f64.argtypes = [_vp, _vp, _i, _vp, _vp]
+    L.rr_flux_f64_culled_range.argtypes = ([_vp, _vp, _i, _vp, _i, _vp, _i, _vp, _i, _i, _i, _vp, _vp, _vp, _vp,
+                                            _vp, _vp, _i, _d, _vp, _i, _i, _vp, _i, _vp])
     L.rr_flux_f64_range.argtypes = ([_vp, _i, _vp, _i, _vp, _i, _vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i,
                                      _d, _vp, _i, _i, _vp, _i, _vp])
     L.rr_ts_workspace_bytes.argtypes = [_i, _i, _i, _i]

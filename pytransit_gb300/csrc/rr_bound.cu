@@ -4,7 +4,8 @@
 // arithmetic, model_full.py:75-99 and model_trspec.py:72-93, to ~1e-15).
 //
 // The bound is built from the split path's own prologue tables and the FP64
-// parameters, one warp per parameter vector:
+// parameters (the FP64 jet a lane per parameter vector, the rest a warp per
+// parameter vector):
 //   * the z error: the FP32 Taylor coefficients against the FP64 jet
 //     recomputed here (the difference itself, not an estimate of it) summed
 //     over the bounding box, |t|^j sum_j |dc_j|, plus the FP32 Horner, the
@@ -45,9 +46,10 @@ struct BoundArgs {
   unsigned long long* bound_max; // max over pv (bits of a non-negative double), zeroed by the caller
 };
 
-// The z error of pv on |t| <= tb (lane 0 only): the FP32 coefficients of the
+// The z error of pv on |t| <= tb, without the square root's term
+// 4u (1 + kmax), which the per-pv pass adds: the FP32 coefficients of the
 // record against the FP64 jet.
-__device__ inline double z_error(const BoundArgs& B, int pv, const float* c32, double tb, double kmax) {
+__device__ inline double z_error_part(const BoundArgs& B, int pv, const float* c32, double tb) {
   double c[10];
   solve2d_conj(B.p[pv], B.a[pv], B.inc[pv], B.e[pv], B.w[pv], c);
   double dcz = 0.0, M = 0.0, V = 0.0, tp = 1.0;
@@ -57,104 +59,135 @@ __device__ inline double z_error(const BoundArgs& B, int pv, const float* c32, d
     if (j < 4) V += (j + 1) * (fabs(c[j + 1]) + fabs(c[6 + j])) * tp;
     tp *= tb;
   }
-  return dcz + 4 * BOUND_U * M + BOUND_U * tb * V + 4 * BOUND_U * (1.0 + kmax) + 1e-11 * V;
+  return dcz + 4 * BOUND_U * M + BOUND_U * tb * V + 1e-11 * V;
 }
 
 // Per-row terms in FP32 (the FP64 rate of this GPU is 1/64 of its FP32
 // rate): every term is a sum of products of non-negative values, so its FP32
 // value is within 16 ulps of the exact one and the result is raised by
-// BOUND_SAFETY.  The z error dz is computed in FP64 (z_error) and rounded up.
+// BOUND_SAFETY.  The z error dz is computed in FP64 and rounded up.
 constexpr float BOUND_SAFETY = 1.0f + 1e-4f;
 
-__global__ void __launch_bounds__(128) error_bound_kernel(BoundArgs B) {
-  const int lane = threadIdx.x & 31;
-  const int pv = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  if (pv >= B.npv) return;   // warp-uniform
+// A block takes one parameter vector per warp (at most 32).  First the FP64
+// part of each z error, one lane of warp 0 per pv, so that every FP64
+// instruction serves up to 32 pvs (the FP64 pipe is the scarce one); then a
+// warp per pv over the LD-table rows.  RoadRunner populations take 32 pvs a
+// block; transmission-spectroscopy ones, with every channel on every row,
+// take 4, which spreads few pvs over more SMs.
+constexpr int BOUND_PV_MAX = 32;
+
+__global__ void __launch_bounds__(BOUND_PV_MAX * 32) error_bound_kernel(BoundArgs B) {
+  __shared__ double s_dz[BOUND_PV_MAX];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int npb_blk = blockDim.x >> 5;   // pvs of this block
+  const int pv0 = blockIdx.x * npb_blk;
   const unsigned FULL = 0xffffffffu;
+  if (warp == 0) {
+    const int pv = pv0 + lane;
+    double part = 0.0;
+    if (lane < npb_blk && pv < B.npv) {
+      if (!B.ts) {
+        const float* o = B.orb + (size_t)pv * ORB32;
+        if (__float_as_int(o[14]) & FLAG_VALID) {
+          const float* L0 = B.lc + (size_t)pv * B.nlc * LC32;
+          double tb = 0.0;
+          for (int lc = 0; lc < B.nlc; ++lc) {
+            const float* r = L0 + (size_t)lc * LC32;
+            tb = fmax(tb, fmax(fabs((double)r[LC_LO]), fabs((double)r[LC_HI])) + 0.5 * r[LC_EXPT]);
+          }
+          part = z_error_part(B, pv, o, tb);
+        }
+      } else {
+        const float* o = B.orb + (size_t)pv * TS_ORB;
+        if (o[15] != 0.0f) {
+          const double tb = fmax(fabs((double)o[10]), fabs((double)o[11])) + 0.5 * B.exptime0;
+          part = z_error_part(B, pv, o, tb);
+        }
+      }
+    }
+    if (lane < npb_blk) s_dz[lane] = part;
+  }
+  __syncthreads();
   const float u = (float)BOUND_U;
   const int ng = B.ng;
   const float dg = (float)B.dg;
-  float worst = 0.0f;
-  if (!B.ts) {
-    const float* o = B.orb + (size_t)pv * ORB32;
-    const bool valid = __float_as_int(o[14]) & FLAG_VALID;
-    if (valid) {
-      const float* L0 = B.lc + (size_t)pv * B.nlc * LC32;
-      double tb = 0.0, kmax = 0.0;
-      for (int lc = 0; lc < B.nlc; ++lc) {
-        const float* r = L0 + (size_t)lc * LC32;
-        tb = fmax(tb, fmax(fabs((double)r[LC_LO]), fabs((double)r[LC_HI])) + 0.5 * r[LC_EXPT]);
-        kmax = fmax(kmax, (double)r[LC_K]);
+  {
+    const int i = warp;
+    const int pv = pv0 + i;
+    if (pv >= B.npv) return;   // warp-uniform
+    float worst = 0.0f;
+    if (!B.ts) {
+      const float* o = B.orb + (size_t)pv * ORB32;
+      const bool valid = __float_as_int(o[14]) & FLAG_VALID;
+      if (valid) {
+        const float* L0 = B.lc + (size_t)pv * B.nlc * LC32;
+        double kmax = 0.0;
+        for (int lc = 0; lc < B.nlc; ++lc) kmax = fmax(kmax, (double)L0[(size_t)lc * LC32 + LC_K]);
+        const float dz = __double2float_ru(s_dz[i] + 4 * BOUND_U * (1.0 + kmax));
+        for (int lc = 0; lc < B.nlc; ++lc) {
+          const float* r = L0 + (size_t)lc * LC32;
+          const float k = r[LC_K], inv_is = fabsf(r[LC_INVIS]);
+          if (!isfinite(inv_is)) continue;   // every in-box value is NaN on both paths
+          const int ns = __float_as_int(r[LC_NS]), pb = __float_as_int(r[LC_PB]);
+          const float* L = B.ldm + ((size_t)pv * B.npb + pb) * ng;
+          const float gz = dg * (1.0f + k), inv_gz = 1.0f / gz, k2 = 2.0f * fminf(k, 1.0f);
+          const float cr = (64 + ns) * u;
+          for (int j = lane; j < ng - 1; j += 32) {
+            const float l0 = L[j], l1 = L[j + 1];
+            const float Lm = fmaxf(fabsf(l0), fabsf(l1)), dL = fabsf(l1 - l0);
+            float kap;
+            const float ai = ccia_star<float>(k, (float)j * gz, kap) * inv_is;
+            const float S = k2 * Lm * inv_is + ai * dL * inv_gz;
+            const float e = cr * Lm * ai + S * dz + 3.0f * u * (float)(j + 1) * dL * ai;
+            worst = fmaxf(worst, e);
+          }
+        }
       }
-      double dz64 = 0.0;
-      if (lane == 0) dz64 = z_error(B, pv, o, tb, kmax);
-      const float dz = __double2float_ru(__shfl_sync(FULL, dz64, 0));
-      for (int lc = 0; lc < B.nlc; ++lc) {
-        const float* r = L0 + (size_t)lc * LC32;
-        const float k = r[LC_K], inv_is = fabsf(r[LC_INVIS]);
-        if (!isfinite(inv_is)) continue;   // every in-box value is NaN on both paths
-        const int ns = __float_as_int(r[LC_NS]), pb = __float_as_int(r[LC_PB]);
-        const float* L = B.ldm + ((size_t)pv * B.npb + pb) * ng;
-        const float gz = dg * (1.0f + k), inv_gz = 1.0f / gz, k2 = 2.0f * fminf(k, 1.0f);
-        const float cr = (64 + ns) * u;
+    } else {
+      const float* o = B.orb + (size_t)pv * TS_ORB;
+      const bool valid = o[15] != 0.0f;
+      if (valid) {
+        const float km = o[12];
+        const float* ch = B.lc + (size_t)pv * B.npb * TS_CH;
+        float afmax = 1.0f;
+        for (int b = lane; b < B.npb; b += 32) afmax = fmaxf(afmax, ch[b * TS_CH]);
+        for (int off = 16; off > 0; off >>= 1) afmax = fmaxf(afmax, __shfl_xor_sync(FULL, afmax, off));
+        const double kmax = (double)km * sqrt((double)afmax);
+        const double dz64 = s_dz[i] + 4 * BOUND_U * (1.0 + kmax);
+        const float dz = __double2float_ru(dz64);
+        // kappa_0 near the outer (inner) contact goes as sqrt(2 eps / (k (1 +- k))):
+        // a z error dz moves it by at most sqrt(2 dz / (k (1 - k)))
+        const float dkap = __double2float_ru(sqrt(2.0 * dz64 / ((double)km * fmax(1.0 - (double)km, 1e-3))));
+        const float cr = (64 + B.nsamples0) * u;
+        const float gz = dg * (1.0f + km), inv_gz = 1.0f / gz;
+        const float ring = 2.0f * float(PI) * km;
+        // lanes over the table rows, the channels inner: the area at the row's
+        // z is shared by every channel
         for (int j = lane; j < ng - 1; j += 32) {
-          const float l0 = L[j], l1 = L[j + 1];
-          const float Lm = fmaxf(fabsf(l0), fabsf(l1)), dL = fabsf(l1 - l0);
           float kap;
-          const float ai = ccia_star<float>(k, (float)j * gz, kap) * inv_is;
-          const float S = k2 * Lm * inv_is + ai * dL * inv_gz;
-          const float e = cr * Lm * ai + S * dz + 3.0f * u * (float)(j + 1) * dL * ai;
-          worst = fmaxf(worst, e);
+          const float A0 = ccia_star<float>(km, (float)j * gz, kap);
+          const float rj = 3.0f * u * (float)(j + 1);
+          const float* L = B.ldm + (size_t)pv * B.npb * ng + j;
+          for (int b = 0; b < B.npb; ++b, L += ng) {
+            const float afac = ch[b * TS_CH], dk = fabsf(ch[b * TS_CH + 1]), inv_is = fabsf(ch[b * TS_CH + 2]);
+            if (!isfinite(inv_is)) continue;
+            const float kb = km * sqrtf(afac);
+            const float l0 = L[0], l1 = L[1];
+            const float Lm = fmaxf(fabsf(l0), fabsf(l1)), dL = fabsf(l1 - l0);
+            const float ai = fmaxf(afac * A0, fmaf(dk, ring, A0)) * inv_is;
+            const float S = 2.0f * fminf(fmaxf(kb, km), 1.0f) * Lm * inv_is + ai * dL * inv_gz;
+            const float e = cr * Lm * ai + S * dz + rj * dL * ai + dk * 2.0f * km * dkap * Lm * inv_is;
+            worst = fmaxf(worst, e);
+          }
         }
       }
     }
-  } else {
-    const float* o = B.orb + (size_t)pv * TS_ORB;
-    const bool valid = o[15] != 0.0f;
-    if (valid) {
-      const float km = o[12];
-      const double tb = fmax(fabs((double)o[10]), fabs((double)o[11])) + 0.5 * B.exptime0;
-      const float* ch = B.lc + (size_t)pv * B.npb * TS_CH;
-      float afmax = 1.0f;
-      for (int b = lane; b < B.npb; b += 32) afmax = fmaxf(afmax, ch[b * TS_CH]);
-      for (int off = 16; off > 0; off >>= 1) afmax = fmaxf(afmax, __shfl_xor_sync(FULL, afmax, off));
-      const double kmax = (double)km * sqrt((double)afmax);
-      double dz64 = 0.0;
-      if (lane == 0) dz64 = z_error(B, pv, o, tb, kmax);
-      dz64 = __shfl_sync(FULL, dz64, 0);
-      const float dz = __double2float_ru(dz64);
-      // kappa_0 near the outer (inner) contact goes as sqrt(2 eps / (k (1 +- k))):
-      // a z error dz moves it by at most sqrt(2 dz / (k (1 - k)))
-      const float dkap = __double2float_ru(sqrt(2.0 * dz64 / ((double)km * fmax(1.0 - (double)km, 1e-3))));
-      const float cr = (64 + B.nsamples0) * u;
-      const float gz = dg * (1.0f + km), inv_gz = 1.0f / gz;
-      const float ring = 2.0f * float(PI) * km;
-      // lanes over the table rows, the channels inner: the area at the row's
-      // z is shared by every channel
-      for (int j = lane; j < ng - 1; j += 32) {
-        float kap;
-        const float A0 = ccia_star<float>(km, (float)j * gz, kap);
-        const float rj = 3.0f * u * (float)(j + 1);
-        const float* L = B.ldm + (size_t)pv * B.npb * ng + j;
-        for (int b = 0; b < B.npb; ++b, L += ng) {
-          const float afac = ch[b * TS_CH], dk = fabsf(ch[b * TS_CH + 1]), inv_is = fabsf(ch[b * TS_CH + 2]);
-          if (!isfinite(inv_is)) continue;
-          const float kb = km * sqrtf(afac);
-          const float l0 = L[0], l1 = L[1];
-          const float Lm = fmaxf(fabsf(l0), fabsf(l1)), dL = fabsf(l1 - l0);
-          const float ai = fmaxf(afac * A0, fmaf(dk, ring, A0)) * inv_is;
-          const float S = 2.0f * fminf(fmaxf(kb, km), 1.0f) * Lm * inv_is + ai * dL * inv_gz;
-          const float e = cr * Lm * ai + S * dz + rj * dL * ai + dk * 2.0f * km * dkap * Lm * inv_is;
-          worst = fmaxf(worst, e);
-        }
-      }
+    for (int off = 16; off > 0; off >>= 1) worst = fmaxf(worst, __shfl_xor_sync(FULL, worst, off));
+    if (lane == 0) {
+      const double bnd = worst > 0.0f ? (double)(worst * BOUND_SAFETY) + BOUND_U : 0.0;
+      B.bound[pv] = bnd;
+      if (B.bound_max) atomicMax(B.bound_max, (unsigned long long)__double_as_longlong(bnd));
     }
-  }
-  for (int off = 16; off > 0; off >>= 1) worst = fmaxf(worst, __shfl_xor_sync(FULL, worst, off));
-  if (lane == 0) {
-    const double bnd = worst > 0.0f ? (double)(worst * BOUND_SAFETY) + BOUND_U : 0.0;
-    B.bound[pv] = bnd;
-    if (B.bound_max) atomicMax(B.bound_max, (unsigned long long)__double_as_longlong(bnd));
   }
 }
 
@@ -169,8 +202,9 @@ static int launch_bounds(BoundArgs& B, void* stream) {
     }
   }
   if (B.npv == 0) return RR_OK;
-  const unsigned nblk = (unsigned)((B.npv + 3) / 4);
-  error_bound_kernel<<<nblk, 128, 0, s>>>(B);
+  const int per = B.ts ? 4 : BOUND_PV_MAX;
+  const unsigned nblk = (unsigned)((B.npv + per - 1) / per);
+  error_bound_kernel<<<nblk, per * 32, 0, s>>>(B);
   return check_launch("rr_error_bounds");
 }
 

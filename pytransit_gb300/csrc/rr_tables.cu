@@ -108,6 +108,45 @@ __global__ void time_split_kernel(const double* __restrict__ times, const int32_
   if (lane == 0) meta[tile] = make_float4(tmin, tmax, __int_as_float(same ? lc0 : -1), 0.0f);
 }
 
+// One warp per 128-point tile: the FP64 summary of the tile for the culled
+// FP64 flux kernel, (earliest time, latest time, light curve or -1 when the
+// tile holds several, 0).
+__global__ void time_tiles_f64_kernel(const double* __restrict__ times, const int32_t* __restrict__ lcids, int npt,
+                                      double* __restrict__ tiles) {
+  const int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int ntiles = (npt + TIME_TILE - 1) / TIME_TILE;
+  if (tile >= ntiles) return;  // warp-uniform
+  double tmin = INFINITY, tmax = -INFINITY;
+  int lc = -2;
+  bool same = true;
+  for (int q = 0; q < 4; ++q) {
+    const int i = tile * TIME_TILE + lane * 4 + q;
+    if (i < npt) {
+      const double t = times[i];
+      tmin = fmin(tmin, t);
+      tmax = fmax(tmax, t);
+      const int l = lcids[i];
+      if (lc == -2) lc = l;
+      same = same && (l == lc);
+    }
+  }
+  const unsigned FULL = 0xffffffffu;
+  for (int o = 16; o > 0; o >>= 1) {
+    tmin = fmin(tmin, __shfl_xor_sync(FULL, tmin, o));
+    tmax = fmax(tmax, __shfl_xor_sync(FULL, tmax, o));
+  }
+  const int lc0 = __shfl_sync(FULL, lc, 0);
+  same = __all_sync(FULL, same && (lc == -2 || lc == lc0));
+  if (lane == 0) {
+    double* o = tiles + 4 * (size_t)tile;
+    o[0] = tmin;
+    o[1] = tmax;
+    o[2] = (same && lc0 >= 0) ? (double)lc0 : -1.0;
+    o[3] = 0.0;
+  }
+}
+
 constexpr int MAX_LDPAR = 16;
 constexpr int NTRAP = 200;
 
@@ -187,6 +226,19 @@ int rr_weights_3d(int nk, double kmin, double kmax, const double* ze, int nz, in
   // dg = gs[1] - gs[0] of gs = linspace(0, 1 - 1e-7, ng)
   if (dg) *dg = (ng == 2) ? (1.0 - 1e-7) : (1.0 - 1e-7) / (double)(ng - 1);
   return check_launch("rr_weights_3d");
+}
+
+size_t rr_time_tiles_f64_doubles(int npt) {
+  if (npt < 0) return 0;
+  return 4 * (((size_t)npt + TIME_TILE - 1) / TIME_TILE);
+}
+
+int rr_time_tiles_f64(const double* times, const int32_t* lcids, int npt, double* tiles64, void* stream) {
+  if (npt < 0 || (npt > 0 && (!times || !lcids || !tiles64))) return RR_ERR_ARG;
+  if (npt == 0) return RR_OK;
+  const int ntiles = (npt + TIME_TILE - 1) / TIME_TILE;
+  time_tiles_f64_kernel<<<(ntiles * 32 + 255) / 256, 256, 0, as_stream(stream)>>>(times, lcids, npt, tiles64);
+  return check_launch("rr_time_tiles_f64");
 }
 
 size_t rr_time_split_floats(int npt) {

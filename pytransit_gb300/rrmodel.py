@@ -110,6 +110,9 @@ class RoadRunnerModel(TransitModel):
         self.host_fill = True
         self.host_threads = _default_host_threads()
         self.host_fill_fraction = 0.5   # share of the rows set to 1 by the host (the rest copied over)
+        # precision='fp64': the fold once per 128-point tile for tiles that
+        # reach no box (the same bits as every point through it, False)
+        self.fp64_cull = True
 
         # Limb darkening model (rrmodel.py:109-131)
         self.ld_law = None           # device law id of a named law, else None
@@ -414,6 +417,19 @@ class RoadRunnerModel(TransitModel):
             comp.wait_stream(cs)
         return 0
 
+    def _flux64(self, L, P, dd, args, istar, npt, npv, nlc, npb, ws, pv0, pv1, out, stream):
+        """The FP64 flux of pvs [pv0, pv1) into their rows out[pv1 - pv0, npt]:
+        tile-culled (rr_flux_f64_culled_range, the same bits) unless fp64_cull
+        is off, then every point through the reference's arithmetic
+        (rr_flux_f64_range)."""
+        k, t0 = args['k'], args['t0']
+        common = (npt, P(k), k.shape[1], P(t0), t0.shape[1], P(args['p']), npv, nlc, npb, P(dd['lcids']),
+                  P(dd['pbids']), P(dd['epids']), P(dd['nsamples']), P(dd['exptimes']), P(istar), self.ng, self.dg,
+                  P(ws), pv0, pv1, P(out), npt, stream)
+        if self.fp64_cull:
+            return L.rr_flux_f64_culled_range(P(dd['time']), P(dd['tiles64']), *common)
+        return L.rr_flux_f64_range(P(dd['time']), *common)
+
     def _flux64_to_host(self, args, dd, istar, npt, npv, nlc, npb, ws, out2d, device, nchunks=8):
         """Plain FP64 flux into the pinned host rows out2d[npv, npt]: the pv
         range in chunks (rr_flux_f64_range) through two device buffers, each
@@ -438,9 +454,7 @@ class RoadRunnerModel(TransitModel):
             b = bufs[c % 2]
             if copied[c % 2] is not None:
                 comp.wait_event(copied[c % 2])
-            st = L.rr_flux_f64_range(P(dd['time']), npt, P(k), k.shape[1], P(t0), t0.shape[1], P(args['p']), npv,
-                                     nlc, npb, P(dd['lcids']), P(dd['pbids']), P(dd['epids']), P(dd['nsamples']),
-                                     P(dd['exptimes']), P(istar), self.ng, self.dg, P(ws), pv0, pv1, P(b), npt, sp)
+            st = self._flux64(L, P, dd, args, istar, npt, npv, nlc, npb, ws, pv0, pv1, b, sp)
             if st != 0:
                 return st
             done = torch.cuda.Event()
@@ -616,10 +630,7 @@ class RoadRunnerModel(TransitModel):
             if st == 0 and pipe:
                 st = self._flux64_to_host(args, dd, istar, npt, npv, nlc, npb, ws, host_rows, device)
             elif st == 0:
-                st = L.rr_flux_f64(P(dd['time']), npt, P(args['k']), k.shape[1], P(args['t0']), t0.shape[1],
-                                   P(args['p']), npv, nlc, npb, P(dd['lcids']), P(dd['pbids']), P(dd['epids']),
-                                   P(dd['nsamples']), P(dd['exptimes']), P(istar), self.ng, self.dg, P(ws),
-                                   P(res), npt, stream)
+                st = self._flux64(L, P, dd, args, istar, npt, npv, nlc, npb, ws, 0, npv, res, stream)
         _lib.check(st, "rr_full")
         self._bound_state = dict(split=split, npv=npv, npb=npb, nlc=nlc, nep=t0.shape[1], ws=ws, device=device,
                                  prm={n: args[n] for n in ('p', 'a', 'i', 'e', 'w')})

@@ -134,6 +134,10 @@ class TransitModel:
                                     device=device)
         _lib.check(L.rr_time_split(_lib.ptr(d['time']), _lib.ptr(d['lcids']), self.npt, d['t_ref'],
                                    _lib.ptr(d['times_ff']), _lib.stream_ptr(device)), "rr_time_split")
+        d['tiles64'] = torch.empty(max(int(L.rr_time_tiles_f64_doubles(self.npt)), 4), dtype=torch.float64,
+                                   device=device)
+        _lib.check(L.rr_time_tiles_f64(_lib.ptr(d['time']), _lib.ptr(d['lcids']), self.npt, _lib.ptr(d['tiles64']),
+                                       _lib.stream_ptr(device)), "rr_time_tiles_f64")
         self._dev = d
         return d
 

@@ -367,3 +367,45 @@ def test_copy_true_through_pinned_rows(precision, host_fill, npv):
     ref = oracle.OracleRoadRunner('quadratic')
     ref.set_data(time)
     assert max_err(got, ref.evaluate(*args)) <= TOL[precision]
+
+
+@pytest.mark.parametrize("ecc,ns", [(False, 1), (True, 7)])
+def test_fp64_culled_equals_plain(ecc, ns):
+    """The tile-culled FP64 flux (precision='fp64', the default) and the plain
+    FP64 kernel (every point through the reference's fold) give the same bits:
+    BJD-scale times in four light curves with their own epochs, exposure
+    times and supersampling, periods from half a day (tiles spanning several
+    epochs) to 15 d, eccentric orbits, an invalid vector, tiles shared by two
+    light curves, and a time array that is not sorted within its tiles."""
+    rng = np.random.default_rng(21 + ns)
+    T = 2459000.0
+    nlc, per = 4, 4001
+    time = np.concatenate([T + 30.0 * j + np.arange(per) * (2.0 / 1440.0) for j in range(nlc)])
+    lcids = np.repeat(np.arange(nlc), per)
+    time[5 * per // 2: 5 * per // 2 + 300] = time[5 * per // 2: 5 * per // 2 + 300][::-1].copy()   # unsorted run
+    npv = 48
+    p = rng.uniform(0.5, 15, npv)
+    a = rng.uniform(3, 20, npv)
+    a[11] = 0.8                                                    # invalid
+    e = rng.uniform(0, 0.3, npv) if ecc else np.zeros(npv)
+    w = rng.uniform(0, 2 * np.pi, npv) if ecc else np.zeros(npv)
+    t0 = T + rng.normal(0, 1e-3, (npv, nlc)) + np.arange(nlc) * 1e-4
+    inc = np.arccos(rng.uniform(0, 0.9, npv) / np.maximum(a, 1.0))
+    args = (rng.uniform(0.05, 0.15, (npv, 1)), np.tile([0.4, 0.2], (npv, nlc, 1)), t0, p, a, inc, e, w)
+    m = rr(precision='fp64')
+    m.set_data(time, lcids=lcids, pbids=np.arange(nlc), nsamples=[ns] * nlc,
+               exptimes=[0.0, 0.02, 0.01, 0.03] if ns > 1 else [0.0] * nlc, epids=np.arange(nlc))
+    m.fp64_cull = False
+    plain = m.evaluate(*args, copy=False).cpu().numpy()
+    m.fp64_cull = True
+    culled = m.evaluate(*args, copy=False).cpu().numpy()
+    np.testing.assert_array_equal(culled, plain)
+    assert np.isnan(culled[11]).all() and (culled < 1.0).any()
+    assert max_err(culled, oracle_eval(time, lcids, nlc, ns, args)) <= TOL['fp64']
+
+
+def oracle_eval(time, lcids, nlc, ns, args):
+    ref = oracle.OracleRoadRunner('quadratic')
+    ref.set_data(time, lcids=lcids, pbids=np.arange(nlc), nsamples=[ns] * nlc,
+                 exptimes=[0.0, 0.02, 0.01, 0.03] if ns > 1 else [0.0] * nlc, epids=np.arange(nlc))
+    return ref.evaluate(*args)
