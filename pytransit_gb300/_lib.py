@@ -129,7 +129,10 @@ def to_host_f64(t, min_points: int = 1 << 17):
     if t.numel() < min_points:
         return t.to(torch.float64).cpu().numpy()
     src = t.to(torch.float64).contiguous()
-    host = torch.empty(src.shape, dtype=torch.float64, pin_memory=True)
+    try:
+        host = torch.empty(src.shape, dtype=torch.float64, pin_memory=True)
+    except RuntimeError:                # no page-locked memory to be had
+        return src.cpu().numpy()
     host.copy_(src, non_blocking=True)
     torch.cuda.current_stream(t.device).synchronize()
     return host.numpy()

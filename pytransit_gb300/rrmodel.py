@@ -585,7 +585,10 @@ class RoadRunnerModel(TransitModel):
                     and user_out.dtype in ((torch.float32, torch.float64) if split else (torch.float64,))):
                 host_rows = user_out.view(npv, npt)
         elif copy and npv * npt >= self.PINNED_RESULT_MIN:
-            host_rows = torch.empty((npv, npt), dtype=torch.float64, pin_memory=True)
+            try:
+                host_rows = torch.empty((npv, npt), dtype=torch.float64, pin_memory=True)
+            except RuntimeError:        # no page-locked memory to be had: copy the device result instead
+                host_rows = None
         pipe = host_rows is not None
         if split:
             ldf = (npt + 3) // 4 * 4
