@@ -274,6 +274,7 @@ def bench_c2(torch, device, steps=5, n_oracle=256):
     res = {}
     for prec in ("split", "fp64"):
         m = RoadRunnerModel('power-2', precision=prec, device=device)
+        m.fp64_cull = False      # the plain FP64 path is the comparator
         m.set_data(**data)
         ms, out = bench_model(m, prm, steps if prec == "split" else 2, torch, device)
         res[prec] = (ms, out)
@@ -296,6 +297,7 @@ def bench_c2(torch, device, steps=5, n_oracle=256):
             "split_points_per_s": pts / (res["split"][0] / 1e3), "fp64_points_per_s": pts / (res["fp64"][0] / 1e3),
             "split_ms": res["split"][0], "fp64_ms": res["fp64"][0],
             "split_over_fp64": res["fp64"][0] / res["split"][0], "max_abs_dF_vs_fp64": dF,
+            "fp64_culled_ms": res["fp64_culled"][0], "fp64_culled_same_bits": culled_same,
             "max_abs_dF_fp64_vs_oracle": float(np.abs(got64 - want).max()),
             "max_abs_dF_split_vs_oracle": float(np.abs(got32 - want).max()),
             "oracle_subset": f"{n_oracle} seeded parameter vectors x all {npt} times ({t_oracle:.1f} s on "
@@ -320,7 +322,12 @@ def bench_ts(torch, device, steps=20, npv=64, npb=200, npt=19700):
     for prec in ("split", "fp64"):
         m = models[prec] = TSModel('quadratic', precision=prec, device=device)
         m.set_data(time_)
+        m.fp64_cull = False      # the plain FP64 path is the comparator
         res[prec] = bench_model(m, prm, steps if prec == "split" else 2, torch, device)
+    # the drop-in's precision='fp64': the same FP64 arithmetic with the fold once per tile
+    models["fp64"].fp64_cull = True
+    res["fp64_culled"] = bench_model(models["fp64"], prm, 5, torch, device)
+    culled_same = bool(torch.equal(res["fp64_culled"][1].nan_to_num(7.0), res["fp64"][1].nan_to_num(7.0)))
     dF = float((res["split"][1].double() - res["fp64"][1]).abs().max().item())
     pts = npv * npb * npt
     out_bytes = pts * 4
@@ -378,6 +385,7 @@ def bench_ts(torch, device, steps=20, npv=64, npb=200, npt=19700):
             "split_points_per_s": pts / (res["split"][0] / 1e3), "fp64_points_per_s": pts / (res["fp64"][0] / 1e3),
             "split_ms": res["split"][0], "fp64_ms": res["fp64"][0],
             "split_over_fp64": res["fp64"][0] / res["split"][0], "max_abs_dF_vs_fp64": dF,
+            "fp64_culled_ms": res["fp64_culled"][0], "fp64_culled_same_bits": culled_same,
             "split_output_gbs": out_bytes / (res["split"][0] / 1e3) / 1e9,
             "split_output_frac_of_hbm": out_bytes / (res["split"][0] / 1e3) / 1e9 / peak,
             "host_ms_per_call": host_ms,
@@ -686,6 +694,7 @@ def per_request_paths(reqs, torch, device, nsample):
             if key not in models:
                 M = TransmissionSpectroscopyModel if kind == 'ts' else RoadRunnerModel
                 models[key] = M(law, precision=prec, device=device)
+                models[key].fp64_cull = False      # the plain FP64 path per request is the comparator
             m = models[key]
             if kind == 'ts':
                 m.set_data(data["time"], nsamples=data["nsamples"], exptimes=data["exptimes"])

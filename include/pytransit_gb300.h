@@ -296,6 +296,14 @@ int rr_ts_prepare_f64_ld(int law, const double *ldc, int npar, const double *mu,
 int rr_ts_flux_f64(const double *times, int npt, const double *t0, const double *p, int npv, int npb, int nsamples0,
                    double exptime0, int ng, double dg, const void *workspace, double *flux, int ldflux,
                    void *stream);
+/* rr_ts_flux_f64 with the fold (model_trspec.py:74-76) once per 128-point
+ * tile for the tiles that reach no box, from the FP64 tile summaries of
+ * rr_time_tiles_f64: the fold is non-decreasing in t with the reference's
+ * rounding, so such a tile is 1.0 at every point; the same bits as
+ * rr_ts_flux_f64. */
+int rr_ts_flux_f64_culled(const double *times, const double *tiles64, int npt, const double *t0, const double *p,
+                          int npv, int npb, int nsamples0, double exptime0, int ng, double dg, const void *workspace,
+                          double *flux, int ldflux, void *stream);
 /* Same, split precision (times_ff and t_ref/t_absmax as rr_full_split). */
 int rr_ts_split(const float *times_ff, double t_ref, double t_absmax, int npt, const double *k,
                 const double *t0, const double *p, const double *a, const double *inc, const double *e,

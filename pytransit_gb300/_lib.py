@@ -83,6 +83,7 @@ def _sig(L):
     L.rr_ts_prepare_f64_ld.argtypes = [_i, _vp, _i, _vp] + _orbit + [_i, _i, _d, _i, _i, _vp, _vp, _sz, _vp]
     L.rr_ts_flux_split.argtypes = [_vp, _i, _i, _i, _i, _d, _i, _d, _vp, _vp, _i, _vp]
     L.rr_ts_flux_f64.argtypes = [_vp, _i, _vp, _vp, _i, _i, _i, _d, _i, _d, _vp, _vp, _i, _vp]
+    L.rr_ts_flux_f64_culled.argtypes = [_vp, _vp, _i, _vp, _vp, _i, _i, _i, _d, _i, _d, _vp, _vp, _i, _vp]
     L.rr_ts_tables.argtypes = [_vp, _i, _i, _i, _i, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]
     L.rr_ts_tables.restype = None
     L.rr_split_error_bounds.argtypes = [_vp] * 5 + [_i, _i, _i, _i, _i, _d, _vp, _vp, _vp, _vp]

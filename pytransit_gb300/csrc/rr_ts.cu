@@ -558,7 +558,7 @@ static int ts_prepare_impl(double t_ref, double t_absmax, const double* k, const
 template <typename R, bool SPLIT>
 static int ts_flux_impl(const double* times, const float* times_ff, int npt, const double* t0, const double* p,
                         int npv, int npb, int nsamples0, double exptime0, int ng, double dg, void* workspace, R* flux,
-                        int ldflux, cudaStream_t s, int pv0 = 0, int pv1 = -1) {
+                        int ldflux, cudaStream_t s, int pv0 = 0, int pv1 = -1, const double* tiles64 = nullptr) {
   TsTables t = carve_ts(workspace, SPLIT, npv, npb, ng);
   if (pv1 < 0) pv1 = npv;
   TsArgs<R> A{};
@@ -574,7 +574,7 @@ static int ts_flux_impl(const double* times, const float* times_ff, int npt, con
   A.flux = flux;
   A.ldflux = ldflux;
   A.npt = npt; A.npb = npb; A.ng = ng; A.nsamples0 = nsamples0;
-  A.exptime0 = exptime0; A.dg = dg;
+  A.exptime0 = exptime0; A.dg = dg; A.tiles64 = tiles64;
   // tile ranges of up to 32 tiles, shorter when the launch would have fewer
   // than about 64 blocks of 4 warps per SM: the short blocks spread the
   // tiles that hold a transit over the SMs (measured: single-tile blocks beat
@@ -651,6 +651,17 @@ int rr_ts_flux_f64(const double* times, int npt, const double* t0, const double*
   if (npv == 0 || npt == 0) return RR_OK;
   return ts_flux_impl<double, false>(times, nullptr, npt, t0, p, npv, npb, nsamples0, exptime0, ng, dg,
                                      const_cast<void*>(workspace), flux, ldflux, as_stream(stream));
+}
+
+int rr_ts_flux_f64_culled(const double* times, const double* tiles64, int npt, const double* t0, const double* p,
+                          int npv, int npb, int nsamples0, double exptime0, int ng, double dg, const void* workspace,
+                          double* flux, int ldflux, void* stream) {
+  int st = ts_check(npt, npv, npb, ng, 1, nsamples0, ldflux, 0, nullptr);
+  if (st) return st;
+  if (npv == 0 || npt == 0) return RR_OK;
+  if (!tiles64) return RR_ERR_ARG;
+  return ts_flux_impl<double, false>(times, nullptr, npt, t0, p, npv, npb, nsamples0, exptime0, ng, dg,
+                                     const_cast<void*>(workspace), flux, ldflux, as_stream(stream), 0, -1, tiles64);
 }
 
 int rr_ts_prepare_split(double t_ref, double t_absmax, const double* k, const double* t0, const double* p,

@@ -55,6 +55,7 @@ struct TsArgs {
   long long ldflux;
   int npt, npb, ng, nsamples0;
   double exptime0, dg;
+  const double* tiles64;      // plain path: FP64 tile summaries (rr_time_tiles_f64) for the tile cull, or null
 };
 
 // Phase-folded time of point pt (time from the nearest conjunction): FP32
@@ -442,6 +443,35 @@ __device__ __forceinline__ void ts_range(const TsArgs<R>& A, int pv, int tb0, in
     return;
   }
   unsigned reach = n >= 32 ? 0xffffffffu : (1u << n) - 1u;
+  if constexpr (!SPLIT) {
+    // The plain path with tile summaries: the reference's FP64 fold
+    // (model_trspec.py:74-76) is non-decreasing in t with its own rounding, so
+    // a tile whose earliest and latest times share an epoch, and whose two
+    // ends' tc miss the box, holds 1.0 at every point (the same bits as the
+    // per-point path).
+    if (A.tiles64) {
+      __syncthreads();                 // S.reach of a previous range is consumed
+      if ((threadIdx.x >> 5) == 0) {
+        const int lane = threadIdx.x & 31;
+        bool hit = false;
+        if (lane < n) {
+          const double* tl = A.tiles64 + 4 * (size_t)(tb0 + lane);
+          const double tz = A.t0[pv], pp = A.p[pv];
+          const double e0 = floor(__ddiv_rn(__dadd_rn(__dsub_rn(tl[0], tz), __dmul_rn(0.5, pp)), pp));
+          const double e1 = floor(__ddiv_rn(__dadd_rn(__dsub_rn(tl[1], tz), __dmul_rn(0.5, pp)), pp));
+          hit = true;
+          if (e0 == e1) {
+            const double c = __dadd_rn(tz, __dmul_rn(e0, pp));
+            hit = !(__dsub_rn(tl[1], c) < (double)o[10] || __dsub_rn(tl[0], c) > (double)o[11]);
+          }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) S.reach = m;
+      }
+      __syncthreads();
+      reach = S.reach;
+    }
+  }
   if constexpr (SPLIT) {
     if (!(o[22] != R(0))) {
       __syncthreads();                 // S.reach of a previous range is consumed

@@ -81,8 +81,12 @@ class TransmissionSpectroscopyModel(RoadRunnerModel):
                 st = L.rr_ts_prepare_f64_ld(self.ld_law, P(args['ldc']), ldc3.shape[2], P(tb['mu']), *orbit, npv,
                                             npb, ex0, self.ng, nz, P(tb['ze']), P(ws), ws.numel(), sp)
                 _lib.check(st, "rr_ts_prepare_f64_ld")
-                st = L.rr_ts_flux_f64(P(dd['time']), npt, P(args['t0']), P(args['p']), npv, npb, ns0, ex0, self.ng,
-                                      self.dg, P(ws), P(out), ldf, sp)
+                if self.fp64_cull:   # the same bits with the fold once per tile that reaches no box
+                    st = L.rr_ts_flux_f64_culled(P(dd['time']), P(dd['tiles64']), npt, P(args['t0']), P(args['p']),
+                                                 npv, npb, ns0, ex0, self.ng, self.dg, P(ws), P(out), ldf, sp)
+                else:
+                    st = L.rr_ts_flux_f64(P(dd['time']), npt, P(args['t0']), P(args['p']), npv, npb, ns0, ex0,
+                                          self.ng, self.dg, P(ws), P(out), ldf, sp)
             _lib.check(st, "rr_ts_flux")
         else:
             if self.ld_law is not None:

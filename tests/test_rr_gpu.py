@@ -409,3 +409,34 @@ def oracle_eval(time, lcids, nlc, ns, args):
     ref.set_data(time, lcids=lcids, pbids=np.arange(nlc), nsamples=[ns] * nlc,
                  exptimes=[0.0, 0.02, 0.01, 0.03] if ns > 1 else [0.0] * nlc, epids=np.arange(nlc))
     return ref.evaluate(*args)
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_pinned_output_multi_lc_supersampled(dtype):
+    """The host-fill output path on the precision workload's shape: light
+    curves of different lengths (tiles shared by two light curves go through
+    the per-point path), 10 supersamples, eccentric orbits, periods down to
+    0.5 d, a vector whose box nears +-p/2 (every point through the exact
+    path), and an invalid one: out= pinned rows equal the device result."""
+    import torch
+    rng = np.random.default_rng(17)
+    T = 2459000.0
+    sizes = [700, 1300, 257, 2100]
+    time = np.concatenate([T + 40.0 * j + np.arange(n) * (30 / 1440) for j, n in enumerate(sizes)])
+    lcids = np.repeat(np.arange(len(sizes)), sizes)
+    npv = 40
+    p = rng.uniform(0.5, 15, npv)
+    a = rng.uniform(3, 20, npv)
+    p[5], a[5] = 0.25, 1.2                   # a transit window that fills most of the period
+    a[9] = 0.9                               # invalid
+    args = (rng.uniform(0.05, 0.15, (npv, 1)), np.stack([rng.uniform(.3, .9, (npv, 4)), rng.uniform(.3, .8, (npv, 4))], -1),
+            T + rng.normal(0, 1e-3, (npv, 1)), p, a, np.arccos(rng.uniform(0, 0.9, npv) / np.maximum(a, 1.0)),
+            rng.uniform(0, 0.3, npv), rng.uniform(0, 2 * np.pi, npv))
+    m = rr('power-2', precision='split')
+    m.set_data(time, lcids=lcids, pbids=np.arange(4), nsamples=[10] * 4, exptimes=[30 / 1440] * 4)
+    want = m.evaluate(*args, copy=False).cpu()
+    tdt = getattr(torch, dtype)
+    out = torch.full((npv, time.size), -7.0, dtype=tdt, pin_memory=True)
+    m.evaluate(*args, out=out)
+    torch.testing.assert_close(out, want.to(tdt), rtol=0, atol=0, equal_nan=True)
+    assert torch.isnan(out[9]).all() and (out[5] < 1).any()

@@ -147,3 +147,37 @@ def test_ts_laws_vs_oracle(precision, law):
     got = m.evaluate(k, ldc, t0, p, a, inc, e, w)
     assert np.sum(want < 1) > 5000
     assert max_err(got, want) <= TOL[precision]
+
+
+@pytest.mark.parametrize("ns,exptime", [(1, 0.0), (5, 0.02)])
+def test_ts_fp64_culled_equals_plain(ns, exptime):
+    """The tile-culled FP64 TS flux (the default with a named law) and the
+    plain one (every point through the reference's fold) give the same bits:
+    a 30-day light curve at 2-min cadence, periods from 0.5 d (tiles spanning
+    several epochs) to 15 d, eccentric orbits, supersampling, an invalid
+    vector; and both match the oracle."""
+    rng = np.random.default_rng(41 + ns)
+    T = 2459000.0
+    time = T + np.arange(21_600) * (2.0 / 1440.0)
+    npv, npb = 12, 24
+    k = rng.uniform(0.09, 0.11, (npv, npb))
+    ldc = np.stack([rng.uniform(0.2, 0.5, (npv, npb)), rng.uniform(0.1, 0.3, (npv, npb))], -1)
+    t0 = T + 3.0 + rng.normal(0, 1e-3, npv)
+    p = rng.uniform(0.5, 15, npv)
+    a = rng.uniform(3, 20, npv)
+    inc = np.arccos(rng.uniform(0, 0.9, npv) / a)
+    e = rng.uniform(0, 0.3, npv)
+    w = rng.uniform(0, 2 * np.pi, npv)
+    a[7] = 0.5
+    m = ts('fp64')
+    m.set_data(time, nsamples=[ns], exptimes=[exptime])
+    m.fp64_cull = False
+    plain = m.evaluate(k, ldc, t0, p, a, inc, e, w, copy=False).cpu().numpy()
+    m.fp64_cull = True
+    culled = m.evaluate(k, ldc, t0, p, a, inc, e, w, copy=False).cpu().numpy()
+    np.testing.assert_array_equal(culled, plain)
+    assert np.isnan(culled[7]).all() and (culled < 1).any()
+    ref = oracle.OracleRoadRunner('quadratic', ts=True)
+    ref.set_data(time, nsamples=[ns], exptimes=[exptime])
+    want = ref.evaluate(k[:4], ldc[:4], t0[:4], p[:4], a[:4], inc[:4], e[:4], w[:4])
+    assert max_err(culled[:4, :, :time.size], want) <= TOL['fp64']
