@@ -515,8 +515,9 @@ def bench_eclipse(torch, device, data, prm, steps=3):
     from pytransit_gb300 import EclipseModel
     args = (prm["k"][:, 0], prm["t0"], prm["p"], prm["a"], prm["i"], prm["e"], prm["w"])
     res, outs = {}, {}
-    for prec, n in (("fp64", steps), ("split", 10 * steps)):
-        m = EclipseModel(precision=prec, device=device)
+    for prec, n in (("fp64", steps), ("fp64_culled", steps), ("split", 10 * steps)):
+        m = EclipseModel(precision="split" if prec == "split" else "fp64", device=device)
+        m.fp64_cull = prec == "fp64_culled"      # the plain FP64 path is the comparator
         m.set_data(data["time"], lcids=data["lcids"], pbids=data["pbids"])
         m.evaluate(*args, copy=False)
         stream = torch.cuda.current_stream(device)
@@ -567,6 +568,8 @@ def bench_eclipse(torch, device, data, prm, steps=3):
                         "CUDA events", "points_per_s": npts / (res["fp64"] * 1e-3), "ms": res["fp64"],
             "split_points_per_s": npts / (res["split"] * 1e-3), "split_ms": res["split"],
             "split_over_fp64": res["fp64"] / res["split"], "max_abs_dF_split_vs_fp64": dmax,
+            "fp64_culled_ms": res["fp64_culled"],
+            "fp64_culled_same_bits": bool(torch.equal(outs["fp64_culled"].nan_to_num(7.0), outs["fp64"].nan_to_num(7.0))),
             "split_device_resident": {"ms_per_step": dev_ms, "points_per_s": npts / (dev_ms * 1e-3),
                                       "output_frac_of_hbm": 4.0 * npts / (dev_ms * 1e-3) / (peak * 1e9),
                                       "timed": "rr_eclipse_split (prologue + flux) through the C ABI, inputs in "

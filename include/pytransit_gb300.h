@@ -383,6 +383,15 @@ int rr_eclipse_f64(const double *times, int npt, const double *k, const double *
                    int npv, int nlc, const int32_t *lcids, const int32_t *epids, const int32_t *nsamples,
                    const double *exptimes, void *workspace, size_t workspace_bytes, double *flux, int ldflux,
                    void *stream);
+/* rr_eclipse_f64 with the fold (model_eclipse.py:70-72) once per 128-point
+ * tile for the tiles that reach no box, from the FP64 tile summaries of
+ * rr_time_tiles_f64: such a tile is pi k^2 at every point, the same bits as
+ * rr_eclipse_f64. */
+int rr_eclipse_f64_culled(const double *times, const double *tiles64, int npt, const double *k, const double *t0,
+                          int ldt0, const double *p, const double *a, const double *inc, const double *e,
+                          const double *w, const double *rstar, int npv, int nlc, const int32_t *lcids,
+                          const int32_t *epids, const int32_t *nsamples, const double *exptimes, void *workspace,
+                          size_t workspace_bytes, double *flux, int ldflux, void *stream);
 /* esmodel (model_ecspec.py:13-63), FP64: flux[npv, npb, ldflux] for the flux
  * ratios fratio[npv, npb], one zero epoch t0[npv], nsamples0 / exptime0. */
 int rr_es_f64(const double *times, int npt, const double *k, const double *t0, const double *p, const double *a,

@@ -60,45 +60,110 @@ __global__ void eclipse_prepare_kernel(const double* __restrict__ k, const doubl
 // eclipse_model's light curve loop (model_eclipse.py:62-80), one thread per
 // (pv, point): pi k^2 outside the padded box, else the mean over the exposure
 // samples of the visible area pi k^2 - A(1, k, z).
-__global__ void __launch_bounds__(256)
-eclipse_flux_kernel(const double* __restrict__ times, int npt, const double* __restrict__ k,
-                    const double* __restrict__ t0, int ldt0, const double* __restrict__ p,
-                    const int32_t* __restrict__ lcids, const int32_t* __restrict__ epids,
-                    const int32_t* __restrict__ nsamples, const double* __restrict__ exptimes,
-                    const double* __restrict__ rec, int npv, double* __restrict__ flux, int ldflux) {
-  const int pv = blockIdx.z * 65535 + blockIdx.y;
-  const int pt = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pt >= npt || pv >= npv) return;
-  const double* o = rec + (size_t)pv * ECL_REC;
-  double* out = flux + (size_t)pv * ldflux + pt;
-  if (o[13] == 0.0) {
-    *out = CUDART_NAN;
-    return;
-  }
-  const int lc = lcids[pt];
-  const double kk = k[pv];
+struct EclF64Args {
+  const double* times;
+  int npt;
+  const double *k, *t0;
+  int ldt0;
+  const double* p;
+  const int32_t *lcids, *epids, *nsamples;
+  const double *exptimes, *rec;
+  int npv;
+  double* flux;
+  int ldflux;
+};
+
+// One point of a valid pv: pi k^2 outside the padded box, else the mean over
+// the exposure samples of the visible area pi k^2 - A(1, k, z).  Compiled
+// once and called by both flux kernels, so that the compiler's fusing of
+// multiplies and adds is the same in both and so are their bits.
+__device__ __noinline__ double ecl_point_f64(const EclF64Args& A, int pv, int pt, const double* o) {
+  const int lc = A.lcids[pt];
+  const double kk = A.k[pv];
   const double pik2 = PI * (kk * kk);
-  const double pp = p[pv];
-  const double te = __dadd_rn(__dadd_rn(t0[(size_t)pv * ldt0 + epids[lc]], o[12]), o[14]);
-  const double t = times[pt];
+  const double pp = A.p[pv];
+  const double te = __dadd_rn(__dadd_rn(A.t0[(size_t)pv * A.ldt0 + A.epids[lc]], o[12]), o[14]);
+  const double t = A.times[pt];
   const double epoch = floor(__ddiv_rn(__dadd_rn(__dsub_rn(t, te), __dmul_rn(0.5, pp)), pp));
   const double tc = __dsub_rn(t, __dadd_rn(te, __dmul_rn(epoch, pp)));
-  const double ex = exptimes[lc];
+  const double ex = A.exptimes[lc];
   const double pad = __dadd_rn(0.003, ex);
-  if (!(__dsub_rn(o[10], pad) <= tc && tc <= __dadd_rn(o[11], pad))) {
-    *out = pik2;
-    return;
-  }
+  if (!(__dsub_rn(o[10], pad) <= tc && tc <= __dadd_rn(o[11], pad))) return pik2;
   double c[10];
   for (int i = 0; i < 10; ++i) c[i] = o[i];
-  const int ns = nsamples[lc];
+  const int ns = A.nsamples[lc];
   double f = 0.0;
   for (int s = 1; s < ns + 1; ++s) {
     const double z = sep_c_f64(tc + ex * ((s - 0.5) / ns - 0.5), c);
     double kap;
     f += pik2 - ccia_star<double>(kk, z, kap);
   }
-  *out = f / ns;
+  return f / ns;
+}
+
+// eclipse_model's light curve loop (model_eclipse.py:62-80), one thread per
+// (pv, point).
+__global__ void __launch_bounds__(256) eclipse_flux_kernel(EclF64Args A) {
+  const int pv = blockIdx.z * 65535 + blockIdx.y;
+  const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pt >= A.npt || pv >= A.npv) return;
+  const double* o = A.rec + (size_t)pv * ECL_REC;
+  A.flux[(size_t)pv * A.ldflux + pt] = o[13] == 0.0 ? CUDART_NAN : ecl_point_f64(A, pv, pt, o);
+}
+
+// The same with the fold once per 128-point tile for tiles that reach no box
+// (tiles64 from rr_time_tiles_f64).  The fold about the eclipse epoch te is
+// non-decreasing in t with the reference's rounding, so a one-light-curve
+// tile whose two ends share an epoch and whose two ends' tc miss the padded
+// box is pi k^2 at every point: the same bits as eclipse_flux_kernel.  A warp
+// tests 32 tiles at once, one per lane.
+constexpr int ECL64_WARPS = 4;
+
+__global__ void __launch_bounds__(ECL64_WARPS * 32) eclipse_flux_culled_kernel(EclF64Args A, const double* tiles64) {
+  const int pv = blockIdx.z * 65535 + blockIdx.y;
+  if (pv >= A.npv) return;   // block-uniform
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = (A.npt + TIME_TILE - 1) / TIME_TILE;
+  const int tbase = (blockIdx.x * ECL64_WARPS + warp) * 32;
+  if (tbase >= ntiles) return;   // warp-uniform
+  const unsigned FULL = 0xffffffffu;
+  const double* o = A.rec + (size_t)pv * ECL_REC;
+  double* row = A.flux + (size_t)pv * A.ldflux;
+  const bool valid = o[13] != 0.0;
+  const double kk = A.k[pv];
+  const int tile = tbase + lane;
+  bool cull = !valid;
+  if (valid && tile < ntiles) {
+    const double tmin = tiles64[4 * (size_t)tile], tmax = tiles64[4 * (size_t)tile + 1];
+    const int lc = (int)tiles64[4 * (size_t)tile + 2];
+    if (lc >= 0) {
+      const double pp = A.p[pv];
+      const double te = __dadd_rn(__dadd_rn(A.t0[(size_t)pv * A.ldt0 + A.epids[lc]], o[12]), o[14]);
+      const double e0 = floor(__ddiv_rn(__dadd_rn(__dsub_rn(tmin, te), __dmul_rn(0.5, pp)), pp));
+      const double e1 = floor(__ddiv_rn(__dadd_rn(__dsub_rn(tmax, te), __dmul_rn(0.5, pp)), pp));
+      if (e0 == e1) {
+        const double c = __dadd_rn(te, __dmul_rn(e0, pp));
+        const double pad = __dadd_rn(0.003, A.exptimes[lc]);
+        cull = __dsub_rn(tmax, c) < __dsub_rn(o[10], pad) || __dsub_rn(tmin, c) > __dadd_rn(o[11], pad);
+      }
+    }
+  }
+  const int jn = min(32, ntiles - tbase);
+  const unsigned jmask = jn == 32 ? FULL : (1u << jn) - 1u;
+  const unsigned cmask = __ballot_sync(FULL, cull) & jmask;
+  const double fill = valid ? PI * (kk * kk) : CUDART_NAN;
+  for (unsigned m = cmask; m; m &= m - 1u) {
+    const int p0 = (tbase + __ffs(m) - 1) * TIME_TILE;
+    for (int q = 0; q < 4; ++q)
+      if (p0 + 32 * q + lane < A.npt) row[p0 + 32 * q + lane] = fill;
+  }
+  for (unsigned m = ~cmask & jmask; m; m &= m - 1u) {
+    const int p0 = (tbase + __ffs(m) - 1) * TIME_TILE;
+    for (int q = 0; q < 4; ++q) {
+      const int pt = p0 + 32 * q + lane;
+      if (pt < A.npt) row[pt] = ecl_point_f64(A, pv, pt, o);
+    }
+  }
 }
 
 // esmodel's light curve loop (model_ecspec.py:49-62), one thread per (pv,
@@ -439,21 +504,48 @@ extern "C" {
 
 size_t rr_eclipse_workspace_bytes(int npv) { return sizeof(double) * (size_t)(npv > 0 ? npv : 1) * ECL_REC + 256; }
 
-int rr_eclipse_f64(const double* times, int npt, const double* k, const double* t0, int ldt0, const double* p,
-                   const double* a, const double* inc, const double* e, const double* w, const double* rstar,
-                   int npv, int nlc, const int32_t* lcids, const int32_t* epids, const int32_t* nsamples,
-                   const double* exptimes, void* workspace, size_t workspace_bytes, double* flux, int ldflux,
-                   void* stream) {
+static int eclipse_f64_launch(const double* times, const double* tiles64, int npt, const double* k, const double* t0,
+                              int ldt0, const double* p, const double* a, const double* inc, const double* e,
+                              const double* w, const double* rstar, int npv, int nlc, const int32_t* lcids,
+                              const int32_t* epids, const int32_t* nsamples, const double* exptimes, void* workspace,
+                              size_t workspace_bytes, double* flux, int ldflux, void* stream) {
   if (npt < 0 || npv < 0 || nlc < 1 || ldt0 < 1 || ldflux < npt) return RR_ERR_ARG;
   if (npv == 0 || npt == 0) return RR_OK;
   if (workspace_bytes < rr_eclipse_workspace_bytes(npv)) return RR_ERR_WORKSPACE;
   cudaStream_t s = as_stream(stream);
   double* rec = static_cast<double*>(workspace);
   eclipse_prepare_kernel<<<(npv + 63) / 64, 64, 0, s>>>(k, p, a, inc, e, w, rstar, npv, rec);
-  dim3 fg((npt + 255) / 256, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
-  eclipse_flux_kernel<<<fg, 256, 0, s>>>(times, npt, k, t0, ldt0, p, lcids, epids, nsamples, exptimes, rec, npv,
-                                         flux, ldflux);
+  EclF64Args A{};
+  A.times = times; A.npt = npt; A.k = k; A.t0 = t0; A.ldt0 = ldt0; A.p = p; A.lcids = lcids; A.epids = epids;
+  A.nsamples = nsamples; A.exptimes = exptimes; A.rec = rec; A.npv = npv; A.flux = flux; A.ldflux = ldflux;
+  if (tiles64) {
+    const int ntiles = (npt + TIME_TILE - 1) / TIME_TILE, per = ECL64_WARPS * 32;
+    dim3 fg((ntiles + per - 1) / per, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
+    eclipse_flux_culled_kernel<<<fg, ECL64_WARPS * 32, 0, s>>>(A, tiles64);
+  } else {
+    dim3 fg((npt + 255) / 256, npv < 65535 ? npv : 65535, (npv + 65534) / 65535);
+    eclipse_flux_kernel<<<fg, 256, 0, s>>>(A);
+  }
   return check_launch("rr_eclipse_f64");
+}
+
+int rr_eclipse_f64(const double* times, int npt, const double* k, const double* t0, int ldt0, const double* p,
+                   const double* a, const double* inc, const double* e, const double* w, const double* rstar,
+                   int npv, int nlc, const int32_t* lcids, const int32_t* epids, const int32_t* nsamples,
+                   const double* exptimes, void* workspace, size_t workspace_bytes, double* flux, int ldflux,
+                   void* stream) {
+  return eclipse_f64_launch(times, nullptr, npt, k, t0, ldt0, p, a, inc, e, w, rstar, npv, nlc, lcids, epids,
+                            nsamples, exptimes, workspace, workspace_bytes, flux, ldflux, stream);
+}
+
+int rr_eclipse_f64_culled(const double* times, const double* tiles64, int npt, const double* k, const double* t0,
+                          int ldt0, const double* p, const double* a, const double* inc, const double* e,
+                          const double* w, const double* rstar, int npv, int nlc, const int32_t* lcids,
+                          const int32_t* epids, const int32_t* nsamples, const double* exptimes, void* workspace,
+                          size_t workspace_bytes, double* flux, int ldflux, void* stream) {
+  if (!tiles64) return RR_ERR_ARG;
+  return eclipse_f64_launch(times, tiles64, npt, k, t0, ldt0, p, a, inc, e, w, rstar, npv, nlc, lcids, epids,
+                            nsamples, exptimes, workspace, workspace_bytes, flux, ldflux, stream);
 }
 
 int rr_es_f64(const double* times, int npt, const double* k, const double* t0, const double* p, const double* a,

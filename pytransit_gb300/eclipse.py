@@ -34,6 +34,8 @@ _SIG = {
     'rr_eclipse_workspace_bytes': ([_i], _sz),
     'rr_eclipse_f64': ([_vp, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz,
                         _vp, _i, _vp], _i),
+    'rr_eclipse_f64_culled': ([_vp, _vp, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp,
+                               _vp, _sz, _vp, _i, _vp], _i),
     'rr_es_f64': ([_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp, _sz, _vp, _i, _vp],
                   _i),
     'rr_eclipse_split_workspace_bytes': ([_i, _i, _i], _sz),
@@ -69,6 +71,9 @@ class _GpuEclipseBase(TransitModel):
             raise ValueError("precision must be 'fp64' or 'split'")
         self.precision = precision
         self.device = device
+        # precision='fp64': the fold once per 128-point tile for tiles that
+        # reach no box (the same bits as every point through it, False)
+        self.fp64_cull = True
 
     def _cuda_device(self):
         return _lib.require_cuda(self.device)
@@ -108,10 +113,13 @@ class EclipseModel(_GpuEclipseBase):
             wsb = L.rr_eclipse_workspace_bytes(npv)
             ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
             out = torch.empty((npv, self.npt), dtype=torch.float64, device=dev)
-            _lib.check(L.rr_eclipse_f64(P(dd['time']), self.npt, P(g['k']), P(g['t0']), t0.shape[1], P(g['p']),
-                                        P(g['a']), P(g['i']), P(g['e']), P(g['w']), P(g['rstar']), npv, self.nlc,
-                                        P(dd['lcids']), P(dd['epids']), P(dd['nsamples']), P(dd['exptimes']), P(ws),
-                                        wsb, P(out), self.npt, _lib.stream_ptr(dev)), "rr_eclipse_f64")
+            rest = (self.npt, P(g['k']), P(g['t0']), t0.shape[1], P(g['p']), P(g['a']), P(g['i']), P(g['e']),
+                    P(g['w']), P(g['rstar']), npv, self.nlc, P(dd['lcids']), P(dd['epids']), P(dd['nsamples']),
+                    P(dd['exptimes']), P(ws), wsb, P(out), self.npt, _lib.stream_ptr(dev))
+            if self.fp64_cull:      # the same bits with the fold once per tile that reaches no box
+                _lib.check(L.rr_eclipse_f64_culled(P(dd['time']), P(dd['tiles64']), *rest), "rr_eclipse_f64")
+            else:
+                _lib.check(L.rr_eclipse_f64(P(dd['time']), *rest), "rr_eclipse_f64")
         if not copy:
             return out
         return np.squeeze(_lib.to_host_f64(out))

@@ -150,3 +150,38 @@ def test_es_split_golden_and_vs_oracle(golden):
     assert f.shape == (npv, npb, time.size)
     assert np.sum(want < 1 - 1e-6) > 10000
     assert _err(f, want) <= SPLIT_TOL
+
+
+@pytest.mark.parametrize("ns", [1, 6])
+def test_eclipse_fp64_culled_equals_plain(ns):
+    """The tile-culled FP64 eclipse flux (EclipseModel's default) and the plain
+    kernel (every point through the reference's fold) give the same bits:
+    three light curves with their own epochs and exposure times, BJD-scale
+    times, periods from 0.5 d to 15 d, eccentric orbits, an invalid vector;
+    and the culled one matches the oracle."""
+    from pytransit_gb300 import EclipseModel
+    rng = np.random.default_rng(50 + ns)
+    T = 2459000.0
+    nlc, per = 3, 3001
+    time = np.concatenate([T + 25.0 * j + np.arange(per) * (4 / 1440) for j in range(nlc)])
+    lcids = np.repeat(np.arange(nlc), per)
+    npv = 24
+    k = rng.uniform(0.05, 0.15, npv)
+    t0 = T + rng.normal(0, 1e-3, (npv, nlc))
+    p = rng.uniform(0.5, 15, npv)
+    a = rng.uniform(3, 20, npv)
+    a[4] = 0.7
+    inc = np.arccos(rng.uniform(0, 0.9, npv) / np.maximum(a, 1.0))
+    e = rng.uniform(0, 0.3, npv)
+    w = rng.uniform(0, 2 * np.pi, npv)
+    ex = [0.0, 0.01, 0.02] if ns > 1 else [0.0] * nlc
+    m = EclipseModel()
+    m.set_data(time, lcids=lcids, nsamples=[ns] * nlc, exptimes=ex, epids=np.arange(nlc))
+    m.fp64_cull = False
+    plain = m.evaluate(k, t0, p, a, inc, e, w, copy=False).cpu().numpy()
+    m.fp64_cull = True
+    culled = m.evaluate(k, t0, p, a, inc, e, w, copy=False).cpu().numpy()
+    np.testing.assert_array_equal(culled, plain)
+    assert np.isnan(culled[4]).all() and (culled[0] < np.pi * k[0] ** 2).any()
+    want = oracle.eclipse_full(time, k, t0, p, a, inc, e, w, 1.0, lcids, np.arange(nlc), [ns] * nlc, ex)
+    assert _err(culled, want) <= TOL
