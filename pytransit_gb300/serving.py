@@ -289,14 +289,23 @@ class WorkItems:
 
     def _make(self, sl):
         i = np.arange(*sl.indices(self.n), dtype=np.int64)
+        out = np.empty((i.size, 4), np.int32)
         if self.by_tiles:
-            pv = i // self.nt
-            t0 = (i % self.nt) * self.per
-            rows = (pv, pv + 1, t0, np.minimum(t0 + self.per, self.ntiles))
+            pv, t = np.divmod(i, self.nt)
+            t *= self.per
+            out[:, 0] = pv
+            out[:, 1] = pv + 1
+            out[:, 2] = t
+            np.minimum(t + self.per, self.ntiles, out=t)
+            out[:, 3] = t
         else:
             pv0 = i * self.per
-            rows = (pv0, np.minimum(pv0 + self.per, self.npv), np.zeros_like(i), np.full_like(i, self.ntiles))
-        return np.stack(rows, 1).astype(np.int32)
+            out[:, 0] = pv0
+            np.minimum(pv0 + self.per, self.npv, out=pv0)
+            out[:, 1] = pv0
+            out[:, 2] = 0
+            out[:, 3] = self.ntiles
+        return out
 
     def __iter__(self):
         return iter(self[:])
