@@ -164,9 +164,12 @@ def shape_request(req: Request):
            for n in ('a', 'i', 'e', 'w')}
     req.npv, req.npt = npv, npt
     req.npb_out = k.shape[1] if req.kind == 'ts' else 1
+    # the time range for the split path's reference time, on the caller's
+    # thread rather than the scheduler's
+    tmin, tmax = (float(time_.min()), float(time_.max())) if npt else (0.0, 0.0)
     req.state['host'] = dict(time=time_, lcids=lcids, pbids=pbids, epids=epids, nsamples=ns, exptimes=ex,
                              k=np.ascontiguousarray(k), ldc=ldc, t0=np.ascontiguousarray(t0), p=pv, nlc=nlc,
-                             npb=npb, **vec)
+                             npb=npb, tmin=tmin, tmax=tmax, **vec)
     return req
 
 
@@ -785,7 +788,7 @@ class GpuExecutor:
         for name, a in arrays:
             o = lo + off[name]
             sv[o:o + a.nbytes] = np.ascontiguousarray(a).reshape(-1).view(np.uint8)
-        tmin, tmax = float(h['time'].min()), float(h['time'].max())
+        tmin, tmax = h['tmin'], h['tmax']
         t_ref = 0.5 * (tmin + tmax)
         t_abs = max(tmax - t_ref, t_ref - tmin)
         base = self.arena.base + blk
