@@ -278,6 +278,13 @@ def bench_c2(torch, device, steps=5, n_oracle=256):
         m.set_data(**data)
         ms, out = bench_model(m, prm, steps if prec == "split" else 2, torch, device)
         res[prec] = (ms, out)
+        if prec == "fp64":
+            # the drop-in's precision='fp64': the same arithmetic, the fold once per tile
+            m.fp64_cull = True
+            ms_c, out_c = bench_model(m, prm, 2, torch, device)
+            culled_same = bool(torch.equal(out_c.nan_to_num(7.0), out.nan_to_num(7.0)))
+            res["fp64_culled"] = (ms_c, None)
+            del out_c
     dF = float((res["split"][1].double() - res["fp64"][1]).abs().max().item())
     # a seeded subset of the population against the oracle (the reference's
     # algorithm in FP64 C on the host cores), on the full C2 data
