@@ -285,3 +285,27 @@ def test_host_fill_from_several_threads_and_after_fork():
     os.kill(pid, 9)
     os.waitpid(pid, 0)
     raise AssertionError("the forked child's fill did not finish")
+
+
+def test_bindings_match_the_header():
+    """Every ctypes binding the package sets up passes as many arguments as the
+    header declares for that entry point (a binding that drifts from the C
+    ABI would pass garbage without an error)."""
+    from pytransit_gb300 import _lib, eclipse, lnlike
+    L = _lib.lib()
+    eclipse._L()
+    lnlike._L()
+    src = open(os.path.join(ROOT, "include", "pytransit_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    decls = re.findall(r"\b(?:int|size_t|void|double)\s+\*?\s*(rr_[a-z0-9_]+)\s*\(([^;]*?)\)\s*;", src, flags=re.S)
+    assert len(decls) >= 50
+    checked = 0
+    for name, args in decls:
+        args = args.strip()
+        n = 0 if args in ("", "void") else len(args.split(","))
+        at = getattr(getattr(L, name), "argtypes", None)
+        if at is None:
+            continue
+        assert len(at) == n, f"{name}: the header declares {n} arguments, the binding passes {len(at)}"
+        checked += 1
+    assert checked >= 45
