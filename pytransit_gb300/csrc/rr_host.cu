@@ -77,18 +77,24 @@ struct FillPool {
 
   void ensure(int nworkers) {
     // a new worker starts from the current generation, so that it takes no
-    // earlier call's task for its own
+    // earlier call's task for its own; a thread that cannot be started (a
+    // process limit) leaves the pool as large as it got
     std::lock_guard<std::mutex> lk(m);
     while (workers < nworkers) {
-      std::thread(&FillPool::worker, this, workers, generation).detach();
+      try {
+        std::thread(&FillPool::worker, this, workers, generation).detach();
+      } catch (...) {
+        return;
+      }
       ++workers;
     }
   }
 
   void run(void* d, size_t nn, double v, bool dbl, int nthreads) {
     std::lock_guard<std::mutex> serial(call);
-    const int np = std::max(1, nthreads);
+    int np = std::max(1, nthreads);
     if (np > 1) ensure(np - 1);
+    np = std::min(np, workers + 1);   // the slices go to the threads there are
     if (np == 1) {
       fill_slice(d, nn, v, dbl, 1, 0);
       return;
