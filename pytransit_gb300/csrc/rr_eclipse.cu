@@ -377,6 +377,8 @@ __global__ void eclipse_prepare_split_kernel(const double* __restrict__ k, const
 // The in-box value of one point: the mean over its samples of the visible
 // planet area pi k^2 - A(1, k, z) (eclipse model) or the mean occulted area
 // A(1, k, z) (spectroscopic model, which applies the channel factors after).
+// For k <= 1/4 the limb's lens area takes the one-arctangent kite form of the
+// transit flux kernel.
 template <bool ES>
 __device__ __forceinline__ float ecl_point(const float* orb, const float* R, float tc) {
   const float k = orb[13], pik2 = orb[15];
@@ -385,8 +387,15 @@ __device__ __forceinline__ float ecl_point(const float* orb, const float* R, flo
   float f = 0.0f;
   for (int s = 0; s < ns; ++s) {
     const float z = sep_c_f32(tc + ex * fmaf((float)s + 0.5f, inv_ns, -0.5f), orb);
-    float kap;
-    const float ar = ccia_star<float>(k, z, kap);
+    float ar;
+    // the kite range of ccia_star (which returns 0 from z = 1 + k on): below
+    // the rounded 1 + k, z - 1 < k and the kite's four factors are positive
+    if (k <= 0.25f && fabsf(1.0f - k) < z && z < 1.0f + k) {
+      ar = kite_star_f32_smallk(k, z);   // a small planet on the limb: one arctangent
+    } else {
+      float kap;
+      ar = ccia_star<float>(k, z, kap);
+    }
     f += ES ? ar : pik2 - ar;
   }
   return f * inv_ns;

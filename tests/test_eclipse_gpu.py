@@ -95,15 +95,18 @@ def test_eclipse_split_golden_and_invalid_rows(golden):
     assert t.dtype == torch.float32 and t.is_cuda
 
 
-def test_eclipse_split_many_pv_vs_oracle_and_fp64():
+@pytest.mark.parametrize("klo,khi", [(0.05, 0.2), (0.25, 0.6)])
+def test_eclipse_split_many_pv_vs_oracle_and_fp64(klo, khi):
     """BJD-scale times (the exact FP32-pair fold), eccentric orbits, 4
-    samples: split against the oracle and against the FP64 kernel."""
+    samples: split against the oracle and against the FP64 kernel.  Radius
+    ratios up to 1/4 take the one-arctangent limb area, larger ones the
+    general lens form."""
     from pytransit_gb300 import EclipseModel
     rng = np.random.default_rng(18)
     T = 2459000.0
     time = T + np.arange(0, 12.0, 5 / 1440)
     npv = 300
-    k = rng.uniform(0.05, 0.2, npv)
+    k = rng.uniform(klo, khi, npv)
     t0 = T + rng.normal(0.3, 1e-3, (npv, 1))
     p = rng.uniform(0.8, 6.0, npv)
     a = rng.uniform(3, 15, npv)
@@ -120,6 +123,36 @@ def test_eclipse_split_many_pv_vs_oracle_and_fp64():
     assert _err(got["fp64"], want) <= TOL
     assert _err(got["split"], want) <= SPLIT_TOL
     assert _err(got["split"], got["fp64"]) <= SPLIT_TOL
+
+
+def test_eclipse_split_full_size_vs_fp64():
+    """The full population of the 8192 pv x 19,700-time workload (4 light
+    curves at 2-min cadence from BJD 2459000, k ~ U(0.05, 0.15), p ~ U(0.5,
+    15) d, a ~ U(3, 20), b ~ U(0, 0.9)): split against the FP64 kernel on
+    the device, 161 M points.  Every split value is finite, and the largest
+    difference is within the split tolerance.  At this size some limb samples
+    land on z = 1 + k rounded, the edge of the lens-area cases."""
+    import torch
+    from pytransit_gb300 import EclipseModel
+    rng = np.random.default_rng(1234)
+    T = 2459000.0
+    npv, npt, nlc = 8192, 19700, 4
+    time = T + np.arange(npt) * (2.0 / 1440.0)
+    lcids = np.minimum((np.arange(npt) * nlc) // npt, nlc - 1)
+    k = rng.uniform(0.05, 0.15, npv)
+    t0 = T + rng.normal(0, 1e-3, (npv, 1))
+    p = rng.uniform(0.5, 15.0, npv)
+    a = rng.uniform(3.0, 20.0, npv)
+    inc = np.arccos(rng.uniform(0.0, 0.9, npv) / a)
+    out = {}
+    for prec in ("split", "fp64"):
+        m = EclipseModel(precision=prec)
+        m.set_data(time, lcids=lcids, pbids=np.arange(nlc))
+        out[prec] = m.evaluate(k, t0, p, a, inc, 0.0, 0.0, copy=False)
+    assert bool(torch.isfinite(out["split"]).all()) and bool(torch.isfinite(out["fp64"]).all())
+    assert float((out["split"].double() - out["fp64"]).abs().max()) <= SPLIT_TOL
+    assert float((out["fp64"] < torch.as_tensor(np.pi * k[:, None] ** 2, device=out["fp64"].device) - 1e-9)
+                 .double().mean()) > 0.01
 
 
 def test_es_split_golden_and_vs_oracle(golden):
