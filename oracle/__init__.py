@@ -2,7 +2,7 @@
 
 CPU FP64 restatement of PyTransit's RoadRunner evaluation path
 (hpparvi/PyTransit 2.8.1), used by tests/, ``__graft_entry__.smoke()`` and the
-CPU-baseline legs of ``bench.py`` as the checker for the CUDA library.
+CPU-baseline legs of ``bench.py`` to check the CUDA library's results.
 
 * ``rr_oracle.c`` restates the numba kernels (common.py, model_full.py,
   model_trspec.py, ldmodels.py) and the missing meepmeep orbit layer; it is

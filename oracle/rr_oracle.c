@@ -2,8 +2,8 @@
  * ORACLE — test infrastructure only.
  *
  * A plain-C, FP64 restatement of PyTransit's RoadRunner evaluation path
- * (reference: hpparvi/PyTransit 2.8.1).  It is the checker for the CUDA
- * library in pytransit_gb300/ and the CPU baseline timed beside it.  Only
+ * (reference: hpparvi/PyTransit 2.8.1).  The tests check the CUDA library in
+ * pytransit_gb300/ against it, and it is the CPU baseline timed beside it.  Only
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs may load
  * it; the product path never does.
  *

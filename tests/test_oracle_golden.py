@@ -178,7 +178,7 @@ def test_taylor_orbit_flux_truncation(eccentric, bound):
     max 4.8e-6 (median 1.1e-8), eccentric max 4.9e-5 (median 1.4e-8), from the
     shortest, closest orbits, where the transit lasts a larger part of the
     period.  This is the degree-4 series itself (meepmeep's), shared by the
-    reference's RoadRunner path, not an error of this build against it."""
+    reference's RoadRunner path, not an error of the CUDA library against it."""
     rng = np.random.default_rng(7)
     worst, per_orbit = 0.0, []
     for _ in range(400):
