@@ -309,3 +309,13 @@ def test_bindings_match_the_header():
         assert len(at) == n, f"{name}: the header declares {n} arguments, the binding passes {len(at)}"
         checked += 1
     assert checked >= 45
+
+
+def test_integration_guide_names_every_entry_point():
+    """Every entry point the header declares is named in INTEGRATION.md, the
+    guide a maintainer of the reference follows to bind the library."""
+    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    names = declared_functions()
+    assert len(names) >= 50
+    missing = [n for n in names if not re.search(r"\b" + n + r"\b", guide)]
+    assert not missing, missing
