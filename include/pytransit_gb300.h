@@ -50,7 +50,9 @@ extern "C" {
 
 int rr_abi_version(void);
 const char *rr_status_string(int status);
-/* Name of the last CUDA error seen by an entry point on this host thread. */
+/* The last error an entry point recorded on this host thread: where it
+ * happened and the CUDA error's text, or the library's own message for some
+ * argument errors; "no error" before the first. */
 const char *rr_last_cuda_error(void);
 
 /* ---- model initialisation ------------------------------------------------ */
