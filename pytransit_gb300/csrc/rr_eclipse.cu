@@ -474,22 +474,53 @@ __global__ void __launch_bounds__(ECL_NW * 32) eclipse_flux_split_kernel(EclSpli
       }
     }
     for (unsigned m = ~cmask & jmask; m; m &= m - 1u) {
-      const int p0 = (tw0 + (j0 + __ffs(m) - 1) * ECL_NW) * TIME_TILE;
+      const int tile = tw0 + (j0 + __ffs(m) - 1) * ECL_NW;
+      const int p0 = tile * TIME_TILE;
       // slot q of lane l: point p0 + q * 32 + l
-      float val[4];
+      const float4 tm = __ldg(meta + tile);              // min hi, max hi, light curve or -1
+      const int tlc = ES ? 0 : __float_as_int(tm.z);     // ES: one record for every point
+      float hi[4], lo[4], val[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int pt = p0 + q * 32 + lane;
+        const float2 tt = pt < A.npt ? __ldg(A.times_ff + pt) : make_float2(0.0f, 0.0f);
+        hi[q] = tt.x;
+        lo[q] = tt.y;
         val[q] = ES ? 0.0f : outv;   // ES: the mean area (0 outside the box)
-        if (pt >= A.npt || !valid) continue;
-        const float2 tt = __ldg(A.times_ff + pt);
-        const float* R = ES ? LCR : LCR + __ldg(A.lcids + pt) * LC32;
-        const float sv = tt.x - R[LC_D0H];
-        const float n = floorf(fmaf(sv, inv_p, 0.5f));
-        const float r = fmaf(-n, p_hi, sv);
-        if (wide || (r >= R[LC_FLO] && r <= R[LC_FHI])) {
-          const float t = exact_tc(tt.x, tt.y, R[LC_D0H], R[LC_D0L], n, p_hi, p_lo);
-          if (R[LC_LO] <= t && t <= R[LC_HI]) val[q] = ecl_point<ES>(orb, R, t);
+      }
+      const float* RT = LCR + (tlc >= 0 ? tlc : 0) * LC32;
+      if (!wide && tlc >= 0 && orb[13] <= 0.25f && (tm.y - tm.x) + fmaxf(-RT[LC_LO], RT[LC_HI]) < 0.5f * p_hi) {
+        // One light curve, and no point of the tile can fold onto another
+        // box copy (span + |box| < p/2): the exact fold once, at the tile's
+        // first point, and each point's exact offset from it, as the transit
+        // flux kernel does.  The time then takes up to two roundings at its
+        // own scale, against one per point below; the area moves with z at
+        // most as 2k, so the tile fold is kept to k <= 1/4 (max |dF| 9.7e-8
+        // against FP64 on the 8192 x 19,700 workload), and larger planets
+        // fold every point.
+        const float h0 = __shfl_sync(FULL, hi[0], 0), l0 = __shfl_sync(FULL, lo[0], 0);
+        const float n0 = floorf(fmaf(h0 - RT[LC_D0H], inv_p, 0.5f));
+        float tail0;
+        const float s0 = exact_tc_pair(h0, l0, RT[LC_D0H], RT[LC_D0L], n0, p_hi, p_lo, tail0);
+        const float blo = RT[LC_LO], bhi = RT[LC_HI];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float t = (s0 + (hi[q] - h0)) + ((lo[q] - l0) + tail0);
+          if (p0 + q * 32 + lane < A.npt && blo <= t && t <= bhi) val[q] = ecl_point<ES>(orb, RT, t);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int pt = p0 + q * 32 + lane;
+          if (pt >= A.npt) continue;
+          const float* R = (ES || tlc >= 0) ? RT : LCR + __ldg(A.lcids + pt) * LC32;
+          const float sv = hi[q] - R[LC_D0H];
+          const float n = floorf(fmaf(sv, inv_p, 0.5f));
+          const float r = fmaf(-n, p_hi, sv);
+          if (wide || (r >= R[LC_FLO] && r <= R[LC_FHI])) {
+            const float t = exact_tc(hi[q], lo[q], R[LC_D0H], R[LC_D0L], n, p_hi, p_lo);
+            if (R[LC_LO] <= t && t <= R[LC_HI]) val[q] = ecl_point<ES>(orb, R, t);
+          }
         }
       }
       for (int b = 0; b < nrow; ++b) {
