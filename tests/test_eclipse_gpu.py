@@ -99,8 +99,8 @@ def test_eclipse_split_golden_and_invalid_rows(golden):
 def test_eclipse_split_many_pv_vs_oracle_and_fp64(klo, khi):
     """BJD-scale times (the exact FP32-pair fold), eccentric orbits, 4
     samples: split against the oracle and against the FP64 kernel.  Radius
-    ratios up to 1/4 take the one-arctangent limb area, larger ones the
-    general lens form."""
+    ratios up to 1/4 take the one-arctangent limb area and one fold per
+    tile, larger ones the general lens form and a fold per point."""
     from pytransit_gb300 import EclipseModel
     rng = np.random.default_rng(18)
     T = 2459000.0
